@@ -1,0 +1,288 @@
+"""Generate the golden fixtures under tests/golden/ by running the OnekaPy reference.
+
+This script is the only committed file that reads the reference tree.  It runs
+in the development container, where the reference sources are mounted; the
+fixtures it writes travel with the repository, and the tests compare against
+them.  It never touches the product package.
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+What it records (all FP64, as the reference computes):
+
+* ``track_<case>.npz``: a small synthetic site, per-realization parameters
+  (K, n, H, discharges, fitted coef_ev / coef_cov and the drawn coef),
+  the release ring, the pre-expanded grid, the reference's chronicle counts
+  (``compute_capturezone`` + ``register``), and every particle's vertices from
+  ``compute_backtrace``.
+* ``expand_<case>.npz``: the same with the reference's auto-expanding grid
+  (no pre-expansion), for the frame replay.
+* ``fit_cases.npz``: ``Model.fit_regional_flow`` on synthetic observation sets.
+* ``raster_cases.npz``: ``ProbabilityField.rasterize`` on random polylines.
+* ``expand_geometry.npz``: ``ProbabilityField.expand`` geometry sequences.
+
+Synthetic sites are seeded; no reference data file is copied.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import platform
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference(path):
+    # Compile the reference from its .py sources into a private cache; the
+    # bytecode shipped inside the reference tree is never read.
+    sys.pycache_prefix = os.path.join(tempfile.gettempdir(), "oneka_ref_pycache")
+    sys.dont_write_bytecode = False
+    sys.path.insert(0, path)
+    np.float = float        # removed from NumPy >= 1.24; the reference still names it
+    from oneka import capturezone, model, probabilityfield
+    return model, capturezone, probabilityfield
+
+
+def make_site(rng, *, nnb, radius, nobs, obs_half, head_fn, sigma, q_target, q_nb, rw=0.25):
+    wells = [(0.0, 0.0, rw, q_target)]
+    for _ in range(nnb):
+        r = radius * np.sqrt(rng.uniform(0.15, 1.0))
+        a = rng.uniform(0, 2 * np.pi)
+        wells.append((float(np.round(r * np.cos(a), 1)), float(np.round(r * np.sin(a), 1)), rw,
+                      q_nb))
+    obs = []
+    for _ in range(nobs):
+        x = float(np.round(rng.uniform(-obs_half, obs_half), 1))
+        y = float(np.round(rng.uniform(-obs_half, obs_half), 1))
+        z = head_fn(x, y) + rng.normal(0, sigma)
+        obs.append((x, y, float(z), sigma))
+    return wells, obs
+
+
+def draw_realizations(M, rng, wells_st, obs, base, kdist, ndist, hdist, nreal):
+    """Per-realization draw, fit and MVN draw, using the reference's own fit."""
+    K, n, H, Q, EV, COV, COEF = [], [], [], [], [], [], []
+    for _ in range(nreal):
+        wells = [(w[0], w[1], w[2], float(rng.uniform(*w[3]))) for w in wells_st]
+        k = float(kdist(rng))
+        nn = float(ndist(rng))
+        h = float(hdist(rng))
+        mo = M.Model(base, k, nn, h, wells)
+        ev, cov = mo.fit_regional_flow(obs, wells[0][0], wells[0][1])
+        ev = np.reshape(ev, [6, ])
+        coef = rng.multivariate_normal(ev, cov)
+        K.append(k); n.append(nn); H.append(h); Q.append([w[3] for w in wells])
+        EV.append(ev); COV.append(cov); COEF.append(coef)
+    return dict(K=np.array(K), n=np.array(n), H=np.array(H), q=np.array(Q), coef_ev=np.array(EV),
+                coef_cov=np.array(COV), coef=np.array(COEF))
+
+
+def release(xt, yt, rt, npaths):
+    pts = []
+    for theta in np.linspace(0, 2 * np.pi, npaths + 1)[0:-1]:
+        pts.append(((rt + 1.0) * np.cos(theta) + xt, (rt + 1.0) * np.sin(theta) + yt))
+    return np.array(pts, dtype=np.float64)
+
+
+def run_track_case(M, C, PF, name, *, wells, obs, base, real, npaths, duration, tol, maxstep,
+                   spacing, umbra, confined, half, preexpand=True, max_vertices_store=None):
+    xt, yt, rt = wells[0][0], wells[0][1], wells[0][2]
+    pf = PF.ProbabilityField(spacing, spacing, xt, yt)
+    if preexpand:
+        pf.expand(xt - half + 0.5 * spacing, xt + half - 0.5 * spacing,
+                  yt - half + 0.5 * spacing, yt + half - 0.5 * spacing)
+    xmin0, ymin0, nr0, nc0 = pf.xmin, pf.ymin, pf.nrows, pf.ncols
+    nreal = len(real["K"])
+    verts, nverts = [], []
+    for r in range(nreal):
+        wl = [(w[0], w[1], w[2], real["q"][r][i]) for i, w in enumerate(wells)]
+        mo = M.Model(base, real["K"][r], real["n"][r], real["H"][r], wl, xt, yt, real["coef"][r])
+        if confined:
+            def feval(xy, mo=mo):
+                Vx, Vy = mo.compute_velocity_confined(xy[0], xy[1])
+                return np.array([-Vx, -Vy])
+        else:
+            def feval(xy, mo=mo):
+                Vx, Vy = mo.compute_velocity(xy[0], xy[1])
+                return np.array([-Vx, -Vy])
+        C.compute_capturezone(xt, yt, rt, npaths, duration, pf, umbra, 1.0, tol, maxstep, feval)
+        for (xs, ys) in release(xt, yt, rt, npaths):
+            v = C.compute_backtrace(xs, ys, duration, tol, maxstep, feval)
+            verts.append(np.array([(float(a[0]), float(a[1])) for a in v], dtype=np.float64))
+            nverts.append(len(v))
+    maxv = max(nverts)
+    V = np.full((len(verts), maxv, 2), np.nan)
+    for i, v in enumerate(verts):
+        V[i, :len(v)] = v
+    out = dict(
+        wells=np.array([w[:3] for w in wells], dtype=np.float64), obs=np.array(obs, dtype=np.float64),
+        base=base, npaths=npaths, duration=duration, tol=tol, maxstep=maxstep, spacing=spacing,
+        umbra=umbra, confined=int(confined), release=release(xt, yt, rt, npaths),
+        grid0=np.array([xmin0, ymin0, spacing, spacing, nr0, nc0], dtype=np.float64),
+        grid=np.array([pf.xmin, pf.ymin, pf.deltax, pf.deltay, pf.nrows, pf.ncols], dtype=np.float64),
+        counts=pf.pgrid.astype(np.int32), total_weight=pf.total_weight,
+        vertices=V.reshape(nreal, npaths, maxv, 2), nvertices=np.array(nverts).reshape(nreal, npaths),
+        **{k: np.asarray(v) for k, v in real.items()})
+    assert np.all(pf.pgrid == np.round(pf.pgrid))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--out", default=HERE)
+    args = ap.parse_args()
+    M, C, PF = import_reference(args.reference)
+    meta = dict(numpy=np.__version__, python=platform.python_version(), machine=platform.machine())
+    print("reference imported;", meta)
+
+    rng = np.random.default_rng(20260101)
+    day = 365.25
+
+    # ---- confined, C1-like: heads from a quadratic read as head, F = 500 m.
+    A, B, Cc, D, E = 1.0e-7, 0.8e-7, 1.0e-8, 1.2e-3, -0.7e-3
+    hf = lambda x, y: A * x * x + B * y * y + Cc * x * y + D * x + E * y + 500.0
+    wells, obs = make_site(rng, nnb=3, radius=2000.0, nobs=25, obs_half=1500.0, head_fn=hf,
+                           sigma=0.1, q_target=(400.0, 600.0), q_nb=(100.0, 500.0))
+    real = draw_realizations(M, rng, wells, obs, 0.0,
+                             lambda g: np.exp(np.log(10.0) + 0.3 * g.normal()),
+                             lambda g: g.uniform(0.2, 0.3), lambda g: g.uniform(20, 30), 3)
+    cases = {}
+    cases["confined_u10"] = run_track_case(
+        M, C, PF, "confined_u10", wells=wells, obs=obs, base=0.0, real=real, npaths=24,
+        duration=10 * day, tol=1, maxstep=10, spacing=10, umbra=10, confined=True, half=2000.0)
+    cases["confined_u20"] = run_track_case(
+        M, C, PF, "confined_u20", wells=wells, obs=obs, base=0.0, real=real, npaths=16,
+        duration=10 * day, tol=1, maxstep=20, spacing=10, umbra=20, confined=True, half=2000.0)
+
+    # ---- mixed: top 30 m, heads straddling the top (general head path).
+    hf2 = lambda x, y: 2e-7 * x * x + 1e-7 * y * y + 1.5e-3 * x - 0.8e-3 * y + 30.5
+    wells2, obs2 = make_site(rng, nnb=5, radius=2500.0, nobs=40, obs_half=2500.0, head_fn=hf2,
+                             sigma=0.1, q_target=(400.0, 600.0), q_nb=(100.0, 400.0))
+    real2 = draw_realizations(M, rng, wells2, obs2, 0.0,
+                              lambda g: np.exp(np.log(10.0) + 0.3 * g.normal()),
+                              lambda g: g.uniform(0.2, 0.3), lambda g: 30.0, 2)
+    cases["mixed_general"] = run_track_case(
+        M, C, PF, "mixed_general", wells=wells2, obs=obs2, base=0.0, real=real2, npaths=16,
+        duration=5 * day, tol=1, maxstep=10, spacing=5, umbra=10, confined=False, half=1500.0)
+
+    # ---- thin unconfined: water table 1-3 m above base, strong pumping: dry cells.
+    # Heads come from a true unconfined potential that includes the wells, so
+    # the water table sits 1-3 m above base next to the target well.
+    nb3 = [(700.0, -400.0, 100.0), (-900.0, 300.0, 80.0), (200.0, 1100.0, 120.0),
+           (-500.0, -1000.0, 60.0)]
+
+    def hf3(x, y, K0=30.0):
+        phi = 2.0e-3 * 30.0 * x + 1.0e-3 * 30.0 * y - 20.0
+        for (xw, yw, qq) in [(0.0, 0.0, 2000.0)] + nb3:
+            phi += qq / (4 * np.pi) * np.log((x - xw) ** 2 + (y - yw) ** 2 + 1e-9)
+        return float(np.sqrt(2.0 * max(phi, 1.0) / K0))
+    wells3, obs3 = make_site(rng, nnb=0, radius=0.0, nobs=30, obs_half=1200.0, head_fn=hf3,
+                             sigma=0.05, q_target=(1800.0, 2200.0), q_nb=None)
+    wells3 += [(xw, yw, 0.25, (0.8 * qq, 1.2 * qq)) for (xw, yw, qq) in nb3]
+    real3 = draw_realizations(M, rng, wells3, obs3, 0.0,
+                              lambda g: g.uniform(25.0, 35.0),
+                              lambda g: g.uniform(0.2, 0.3), lambda g: 20.0, 4)
+    cases["unconfined_thin"] = run_track_case(
+        M, C, PF, "unconfined_thin", wells=wells3, obs=obs3, base=0.0, real=real3, npaths=16,
+        duration=2 * day, tol=1, maxstep=10, spacing=5, umbra=10, confined=False, half=1000.0)
+
+    # ---- the same site with F lowered: some realizations are dry at the ring.
+    real3d = {k: np.array(v, copy=True) for k, v in real3.items()}
+    real3d["coef"][:, 5] -= 450.0
+    cases["unconfined_dryshift"] = run_track_case(
+        M, C, PF, "unconfined_dryshift", wells=wells3, obs=obs3, base=0.0, real=real3d,
+        npaths=16, duration=2 * day, tol=1, maxstep=10, spacing=5, umbra=10, confined=False,
+        half=1000.0)
+    # ---- forward tracking (negative duration) into the pumping well: partial dry traces.
+    cases["forward_dry"] = run_track_case(
+        M, C, PF, "forward_dry", wells=wells3, obs=obs3, base=0.0, real=real3, npaths=16,
+        duration=-20.0, tol=1, maxstep=10, spacing=5, umbra=10, confined=False, half=1000.0)
+
+    # ---- auto-expanding grid (no pre-expansion): the reference grows its grid.
+    cases["expanding_u20"] = run_track_case(
+        M, C, PF, "expanding_u20", wells=wells, obs=obs, base=0.0,
+        real={k: v[:2] for k, v in real.items()}, npaths=12, duration=5 * day, tol=1,
+        maxstep=20, spacing=10, umbra=20, confined=True, half=0.0, preexpand=False)
+
+    for name, d in cases.items():
+        np.savez_compressed(os.path.join(args.out, f"track_{name}.npz"), **d, **meta)
+        print(name, "registered", d["total_weight"], "nonzero", int((d["counts"] > 0).sum()),
+              "max vertices", d["vertices"].shape[2], "grid", d["grid"])
+
+    # ---- forward and backward single traces via compute_backtrace.
+    mo = M.Model(0.0, 10.0, 0.25, 25.0, [(0.0, 0.0, 0.25, 500.0), (300.0, -200.0, 0.25, 200.0)],
+                 0.0, 0.0, real["coef"][0])
+    feval = lambda xy: -np.array(mo.compute_velocity_confined(xy[0], xy[1]))
+    tr = []
+    for (xs, ys, dur) in [(40.0, 10.0, -20.0), (-60.0, 35.0, -45.0), (20.0, -15.0, 400.0)]:
+        v = C.compute_backtrace(xs, ys, dur, 1, 5, feval)
+        tr.append(np.array([(float(a[0]), float(a[1])) for a in v]))
+    maxv = max(len(v) for v in tr)
+    TV = np.full((len(tr), maxv, 2), np.nan)
+    for i, v in enumerate(tr):
+        TV[i, :len(v)] = v
+    np.savez_compressed(os.path.join(args.out, "backtrace_cases.npz"), vertices=TV,
+                        nvertices=np.array([len(v) for v in tr]), coef=real["coef"][0],
+                        starts=np.array([(40.0, 10.0, -20.0), (-60.0, 35.0, -45.0), (20.0, -15.0, 400.0)]),
+                        **meta)
+
+    # ---- fits: confined, mixed and unconfined observation sets.
+    fit_rows = []
+    for (wl, ob, base, K, H) in [(wells, obs, 0.0, 12.0, 25.0), (wells2, obs2, 0.0, 9.0, 30.0),
+                                 (wells3, obs3, 0.0, 30.0, 20.0)]:
+        wq = [(w[0], w[1], w[2], 0.5 * (w[3][0] + w[3][1])) for w in wl]
+        mo = M.Model(base, K, 0.25, H, wq)
+        ev, cov = mo.fit_regional_flow(ob, wq[0][0], wq[0][1])
+        fit_rows.append(dict(wells=np.array(wq), obs=np.array(ob), base=base, K=K, H=H,
+                             ev=np.reshape(ev, [6]), cov=cov))
+    np.savez_compressed(os.path.join(args.out, "fit_cases.npz"),
+                        **{f"{k}_{i}": v for i, d in enumerate(fit_rows) for k, v in d.items()},
+                        ncases=len(fit_rows), **meta)
+
+    # ---- rasterize: random polylines on a fixed window (incl. zero-length and off-grid).
+    rr = np.random.default_rng(7)
+    polys, grids, rgrids = [], [], []
+    for k in range(12):
+        sp = [2.0, 5.0, 10.0, 2.5][k % 4]
+        um = sp * [1.0, 2.0, 1.5][k % 3]
+        pf = PF.ProbabilityField(sp, sp, 0.0, 0.0)
+        pf.expand(-300.0, 300.0, -200.0, 250.0)
+        n = int(rr.integers(1, 40))
+        start = rr.uniform(-250, 250, size=2)
+        steps = rr.normal(0, 8.0, size=(n - 1, 2))
+        if k % 5 == 0 and n > 3:
+            steps[1] = 0.0                      # zero-length segment
+        if k % 4 == 3:
+            start = np.array([290.0, -190.0])   # runs off the grid edge
+        pts = np.vstack([start, start + np.cumsum(steps, axis=0)]) if n > 1 else start[None, :]
+        pf.rasterize(list(pts[:, 0]), list(pts[:, 1]), um)
+        polys.append(np.pad(pts, ((0, 40 - len(pts)), (0, 0)), constant_values=np.nan))
+        grids.append([pf.xmin, pf.ymin, pf.deltax, pf.deltay, pf.nrows, pf.ncols, um, len(pts)])
+        rgrids.append(np.packbits(pf.rgrid.reshape(-1)))
+    np.savez_compressed(os.path.join(args.out, "raster_cases.npz"), polys=np.array(polys),
+                        grids=np.array(grids), **{f"rgrid_{i}": g for i, g in enumerate(rgrids)},
+                        **meta)
+
+    # ---- expand geometry sequences.
+    seqs = []
+    for (dx, xo, yo, boxes) in [(1.0, 100.0, 50.0, [(100.0, 200.0, 50.0, 100.0), (150.0, 175.0, 75.0, 100.0)]),
+                                (2.5, 0.3, -7.1, [(-40.2, 13.3, -9.0, 40.7), (-80.0, -79.0, 100.0, 101.0)]),
+                                (0.7, 1234.567, 89.01, [(1200.0, 1300.0, 50.0, 60.0)])]:
+        pf = PF.ProbabilityField(dx, dx, xo, yo)
+        geo = []
+        for b in boxes:
+            pf.expand(*b)
+            geo.append([pf.xmin, pf.xmax, pf.ymin, pf.ymax, pf.nrows, pf.ncols])
+        seqs.append(dict(dx=dx, xo=xo, yo=yo, boxes=np.array(boxes), geo=np.array(geo)))
+    np.savez_compressed(os.path.join(args.out, "expand_geometry.npz"),
+                        **{f"{k}_{i}": v for i, d in enumerate(seqs) for k, v in d.items()},
+                        ncases=len(seqs), **meta)
+    print("done")
+
+
+if __name__ == "__main__":
+    main()
