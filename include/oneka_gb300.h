@@ -1,0 +1,251 @@
+/*
+ * oneka_gb300.h -- C ABI of liboneka_gb300.so, the GB300 (sm_103a) engine for
+ * OnekaPy's per-realization hot path:
+ *
+ *   realization draw -> weighted least-squares fit of A..F -> multivariate-
+ *   normal draw -> Dormand-Prince backtrace of npaths particles -> chronicle
+ *   of every trace into the ProbabilityField grid.
+ *
+ * The OnekaPy reference (Python/NumPy, single thread) has no FFI; its
+ * operator surface is the Python functions cited beside each entry point.
+ * These entry points are what a binding of that surface calls (ctypes,
+ * cffi, or a C/C++ host).
+ *
+ * Conventions
+ *   - Every array pointer is a DEVICE pointer owned by the caller unless the
+ *     comment says "host".  Struct arguments themselves live in host memory.
+ *   - Calls are ordered on `stream` (a cudaStream_t; NULL = legacy default
+ *     stream) and return ONEKA_OK (0) or a negative ONEKA_ERR_* code.  They
+ *     never abort the process.  oneka_last_error() describes the last failure
+ *     of the calling thread.
+ *   - Per-particle and per-realization outcomes are status codes, not errors:
+ *     a dry cell ends a trace with the vertices so far (the reference's
+ *     AquiferError path), and an attempt cap ends a trace that would never
+ *     finish (the reference loops forever on a NaN velocity).
+ *   - Arrays are row-major and C-contiguous.
+ */
+#ifndef ONEKA_GB300_H
+#define ONEKA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ONEKA_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define ONEKA_API __attribute__((visibility("default")))
+#else
+#define ONEKA_API
+#endif
+
+/* return codes */
+#define ONEKA_OK 0
+#define ONEKA_ERR_INVALID (-1)   /* bad argument (null pointer, size, option) */
+#define ONEKA_ERR_CUDA (-2)      /* a CUDA launch or runtime call failed */
+#define ONEKA_ERR_SCRATCH (-3)   /* scratch buffer too small for one realization slot */
+
+/* per-realization status (oneka_realize; skipped by oneka_track) */
+#define ONEKA_REAL_OK 0
+#define ONEKA_REAL_RANGE 1       /* an observed head is at or below the base (model.py:558-559 RangeError) */
+#define ONEKA_REAL_NOT_SPD 2     /* normal equations not positive definite (model.py:604 LinAlgError) */
+
+/* per-particle status (oneka_track) */
+#define ONEKA_TRACE_OK 0         /* reached |duration| */
+#define ONEKA_TRACE_DRY 1        /* potential <= 0 or head <= 0 (model.py:343, :380 AquiferError) */
+#define ONEKA_TRACE_STEP_LIMIT 2 /* attempt cap reached */
+
+/* distribution kinds (generate_random_variate, stochastic.py:297-304; LOGNORMAL is an extension) */
+#define ONEKA_DIST_CONST 0       /* p0 */
+#define ONEKA_DIST_UNIFORM 1     /* U(p0, p1) */
+#define ONEKA_DIST_TRIANGULAR 2  /* (min p0, mode p1, max p2) */
+#define ONEKA_DIST_LOGNORMAL 3   /* exp(N(mu = p0, sigma = p1)) */
+
+/* oneka_realize modes */
+#define ONEKA_MODE_STOCHASTIC 0  /* draw q, K, n, H; fit; draw A..F (stochastic.py:220-241) */
+#define ONEKA_MODE_MEAN 1        /* distribution means; fit; A..F = fitted mean (deterministic.py:175-199) */
+#define ONEKA_MODE_GIVEN 2       /* q and aquifer are inputs; fit; draw A..F */
+#define ONEKA_MODE_GIVEN_EV 3    /* q and aquifer are inputs; fit; A..F = fitted mean */
+
+/* oneka_track precision */
+#define ONEKA_FP64 0             /* parity build: the reference's FP64 arithmetic, bit-exact counts */
+#define ONEKA_FP32 1             /* fast build: FP32 tracking, FP64 where digits are lost */
+
+typedef struct OnekaDist {
+    int32_t kind;
+    int32_t pad;
+    double p0, p1, p2;
+} OnekaDist;
+
+/* One site: wells, observations and the regional-flow origin. */
+typedef struct OnekaSite {
+    int32_t nwells;          /* wells in the reference's list order */
+    int32_t nobs;
+    int32_t target;          /* index of the target well (centre of the release ring) */
+    int32_t pad;
+    double base;             /* aquifer base elevation [m] */
+    double xo, yo;           /* regional-flow origin; the stochastic driver uses the target well.
+                                The FP32 tracker measures coordinates from it. */
+    const double* wells;     /* [nwells][3]: xw, yw, rw */
+    const double* obs;       /* [nobs][4]: x, y, z_ev, z_std (may be NULL when nobs == 0) */
+} OnekaSite;
+
+/* Per-realization parameters, structure of arrays ([nreal] leading). */
+typedef struct OnekaRealizations {
+    double* coef;            /* [nreal][6] A..F used for tracking */
+    double* coef_ev;         /* [nreal][6] fitted expected value, or NULL */
+    double* coef_cov;        /* [nreal][36] fitted covariance, or NULL */
+    double* q;               /* [nreal][nwells] well discharges [m^3/d] */
+    double* aquifer;         /* [nreal][3] conductivity, porosity, thickness */
+    int32_t* status;         /* [nreal] ONEKA_REAL_* */
+} OnekaRealizations;
+
+/* Node grid: node (i, j) at (xmin + j*dx, ymin + i*dy), i < nrows, j < ncols. */
+typedef struct OnekaGrid {
+    double xmin, ymin, dx, dy;
+    int32_t nrows, ncols;
+} OnekaGrid;
+
+/*
+ * The grid a particle's trace is rasterized against when the caller replays
+ * the reference's auto-expanding ProbabilityField: its origin at that time
+ * and its offset (columns, rows) inside the final grid.
+ */
+typedef struct OnekaFrame {
+    double xmin, ymin;
+    int32_t coff, roff;
+    int32_t ncols, nrows;
+} OnekaFrame;
+
+typedef struct OnekaTrackOpts {
+    double duration;         /* [d]; negative tracks forward (capturezone.py:143) */
+    double tol;              /* local error tolerance [m] */
+    double maxstep;          /* maximum space step [m] */
+    double umbra;            /* vector-to-raster range [m] */
+    int32_t confined;        /* 1: compute_velocity_confined; 0: compute_velocity */
+    int32_t precision;       /* ONEKA_FP64 or ONEKA_FP32 */
+    int32_t max_attempts;    /* step attempts per particle before STEP_LIMIT; <= 0: 1,000,000 */
+    int32_t block;           /* threads per block, multiple of 32; 0: library default */
+} OnekaTrackOpts;
+
+/* Optional per-particle outputs ([nreal][npaths] leading); any pointer may be NULL. */
+typedef struct OnekaTrackOut {
+    double* endpoint;        /* [..][2] last vertex */
+    double* bbox;            /* [..][4] xmin, xmax, ymin, ymax over the vertices */
+    int32_t* naccept;        /* accepted steps */
+    int32_t* nattempt;       /* attempted steps */
+    int32_t* status;         /* ONEKA_TRACE_* */
+    double* vertices;        /* [..][max_vertices][2] first vertices of each trace */
+    int32_t* nvertices;      /* vertices in the full trace (may exceed max_vertices) */
+    int32_t max_vertices;
+    int32_t pad;
+    int64_t* counters;       /* [4] summed over all particles: step attempts, accepted steps,
+                                chronicle node tests, chronicle word atomics; or NULL */
+} OnekaTrackOut;
+
+/* ---------------------------------------------------------------------- */
+
+/* ABI version of the loaded library (ONEKA_ABI_VERSION). */
+ONEKA_API int oneka_abi_version(void);
+
+/* Description of the last failure on the calling thread ("" if none). */
+ONEKA_API const char* oneka_last_error(void);
+
+/*
+ * log(r^2) from every observation to every well, [nobs][nwells], FP64.
+ * The fit reuses it for every realization of the site; the well term of the
+ * observation potential is then (q * logr2) * 1/(4 pi) in the reference's
+ * order (model.py:258-264).
+ */
+ONEKA_API int oneka_site_logr2(const OnekaSite* site, double* logr2, void* stream);
+
+/*
+ * Realization draw + WLS fit + MVN draw for realizations
+ * [first, first + nreal) of the Philox stream `seed` (one warp each).
+ *   stochastic.py:220-241 (draws, fit, MVN); model.py:497-606 (FOSM rows,
+ *   lstsq + inv, here FP64 normal equations with a Jacobi-scaled Cholesky
+ *   factor; the MVN draw uses the same factor).
+ *   qdist: [nwells] distributions of the discharges; adist: host [3] for
+ *   conductivity, porosity, thickness.  logr2 from oneka_site_logr2, or NULL.
+ *   For ONEKA_MODE_GIVEN*, out->q and out->aquifer are read, not written.
+ */
+ONEKA_API int oneka_realize(const OnekaSite* site, const OnekaDist* qdist, const OnekaDist* adist,
+                  const double* logr2, uint64_t seed, uint64_t first, int32_t nreal,
+                  int32_t mode, OnekaRealizations* out, void* stream);
+
+/* Bytes of scratch oneka_track needs for `slots` realizations in flight. */
+ONEKA_API size_t oneka_track_scratch_bytes(const OnekaGrid* grid, int32_t slots);
+
+/*
+ * Backtrack npaths particles for each realization and chronicle the traces.
+ *   capturezone.py:51-253 (release ring given as `release` [npaths][2];
+ *   Dormand-Prince 5(4) with the reference's step control), model.py:207-427
+ *   (velocity), probabilityfield.py:264-372 (rasterize within umbra,
+ *   per-realization OR, register with weight 1).
+ *   counts [nrows][ncols] int32 is incremented once per realization for each
+ *   node any of its traces marks; `registered` (int64, may be NULL) is
+ *   incremented once per realization tracked (status ONEKA_REAL_OK).
+ *   frames: [nreal][npaths] or NULL (every trace against `grid`).
+ *   scratch (16-byte aligned) holds realization slots of
+ *   oneka_track_scratch_bytes(grid, 1) bytes each (a bitmask of
+ *   ceil(ncols/32) words per row plus a small header).  It must be all
+ *   zero on entry (zero it once after allocating it):
+ *     counts != NULL: working slots, at least one; more slots let more
+ *       realizations run per launch.  Every slot used is zero again on
+ *       return, so the same scratch serves the next call as it is.
+ *     counts == NULL, scratch != NULL ("mark only"): realization k ORs its
+ *       traces into slot k (nreal slots needed); nothing is cleared or
+ *       registered, so the caller can register with a weight
+ *       (oneka_register_weighted).
+ *     both NULL: tracking only, for the per-particle outputs.
+ */
+ONEKA_API int oneka_track(const OnekaSite* site, const OnekaRealizations* real, int32_t nreal,
+                const double* release, int32_t npaths, const OnekaTrackOpts* opts,
+                const OnekaGrid* grid, const OnekaFrame* frames, int32_t* counts,
+                int64_t* registered, const OnekaTrackOut* out, void* scratch,
+                size_t scratch_bytes, void* stream);
+
+/*
+ * Model evaluation at npts points (model.py:207-427): potential, discharge
+ * [npts][2], head, velocity [npts][2] (general when confined == 0, else the
+ * confined shortcut) and status (ONEKA_TRACE_DRY where the reference raises
+ * AquiferError).  Any output may be NULL.  coef is host [6].
+ */
+ONEKA_API int oneka_evaluate(const OnekaSite* site, const double* q, double conductivity, double porosity,
+                   double thickness, const double* coef, const double* points, int64_t npts,
+                   int32_t confined, double* potential, double* discharge, double* head,
+                   double* velocity, int32_t* status, void* stream);
+
+/*
+ * ProbabilityField.rasterize (probabilityfield.py:313-339) without expand:
+ * OR the nodes within umbra of the polyline xy [n][2] into `mask`, a
+ * realization bitmask of oneka_track_scratch_bytes(grid, 1) bytes
+ * (row-major, ceil(ncols/32) words per row).  frame may be NULL.
+ */
+ONEKA_API int oneka_rasterize(const OnekaGrid* grid, const OnekaFrame* frame, const double* xy, int64_t n,
+                    double umbra, uint32_t* mask, void* stream);
+
+/*
+ * ProbabilityField.register (probabilityfield.py:357-359) for one bitmask:
+ * pgrid[marked] += weight, then the mask is cleared.
+ */
+ONEKA_API int oneka_register_weighted(const OnekaGrid* grid, uint32_t* mask, double weight, double* pgrid,
+                            void* stream);
+
+/*
+ * Measurement helper (no reference counterpart): sustained FMA throughput of
+ * this GPU in FLOP/s for FP32 (fp64 == 0) or FP64 (fp64 != 0), from a
+ * register-resident FMA loop over every SM.  Synchronizes `stream`.
+ */
+ONEKA_API int oneka_fma_peak(int32_t fp64, double* flops_per_s, void* stream);
+
+/* ProbabilityField.distancesquared (probabilityfield.py:380-427) for n queries [n][6]. */
+ONEKA_API int oneka_distancesquared(const double* abc, double* d2, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ONEKA_GB300_H */

@@ -1,0 +1,244 @@
+// capi.cu -- extern "C" entry points of liboneka_gb300.so (include/oneka_gb300.h).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "oneka_internal.cuh"
+
+namespace oneka {
+
+cudaError_t launch_realize(const OnekaSite& site, const OnekaDist* qdist, const OnekaDist* adist,
+                           const double* logr2, unsigned long long seed, unsigned long long first,
+                           int nreal, int mode, const OnekaRealizations& out, cudaStream_t s);
+cudaError_t launch_logr2(const OnekaSite& site, double* logr2, cudaStream_t s);
+cudaError_t launch_register_weighted(uint32_t* mask, const OnekaGrid& g, double weight, double* pgrid,
+                                     cudaStream_t s);
+cudaError_t launch_rasterize(const OnekaGrid& g, const OnekaFrame& f, const double* xy, long long n,
+                             double umbra, uint32_t* mask, cudaStream_t s);
+cudaError_t launch_distancesquared(const double* abc, double* d2, long long n, cudaStream_t s);
+cudaError_t probe_fma(int fp64, double* flops_per_s, cudaStream_t s);
+cudaError_t launch_evaluate(const OnekaSite& site, const double* q, double K, double n, double H,
+                            const double* coef, const double* pts, long long npts, int confined,
+                            double* potential, double* discharge, double* head, double* velocity,
+                            int32_t* status, cudaStream_t s);
+
+static thread_local char g_err[512];
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+}  // namespace oneka
+
+using namespace oneka;
+
+#define ONEKA_CHECK_ARG(cond, msg)          \
+    do {                                    \
+        if (!(cond)) {                      \
+            set_error("invalid argument: %s", msg); \
+            return ONEKA_ERR_INVALID;       \
+        }                                   \
+    } while (0)
+
+#define ONEKA_CHECK_CUDA(expr)                                                  \
+    do {                                                                        \
+        cudaError_t e_ = (expr);                                                \
+        if (e_ != cudaSuccess) {                                                \
+            set_error("%s: %s", #expr, cudaGetErrorString(e_));                \
+            return ONEKA_ERR_CUDA;                                              \
+        }                                                                       \
+    } while (0)
+
+static bool grid_ok(const OnekaGrid* g) {
+    return g && g->nrows > 0 && g->ncols > 0 && g->dx > 0 && g->dy > 0;
+}
+
+extern "C" {
+
+int oneka_abi_version(void) { return ONEKA_ABI_VERSION; }
+
+const char* oneka_last_error(void) { return g_err; }
+
+int oneka_site_logr2(const OnekaSite* site, double* logr2, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(site && logr2, "site/logr2");
+    ONEKA_CHECK_ARG(site->nwells >= 0 && site->nobs >= 0, "sizes");
+    ONEKA_CHECK_ARG(site->nobs == 0 || (site->obs && site->wells), "site arrays");
+    ONEKA_CHECK_CUDA(launch_logr2(*site, logr2, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_realize(const OnekaSite* site, const OnekaDist* qdist, const OnekaDist* adist,
+                  const double* logr2, uint64_t seed, uint64_t first, int32_t nreal, int32_t mode,
+                  OnekaRealizations* out, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(site && out && adist, "site/out/adist");
+    ONEKA_CHECK_ARG(nreal >= 0, "nreal");
+    ONEKA_CHECK_ARG(mode >= ONEKA_MODE_STOCHASTIC && mode <= ONEKA_MODE_GIVEN_EV, "mode");
+    ONEKA_CHECK_ARG(site->nwells >= 1 && site->nwells <= 4096, "nwells must be in [1, 4096]");
+    ONEKA_CHECK_ARG(site->nobs >= 0 && (site->nobs == 0 || site->obs), "observations");
+    ONEKA_CHECK_ARG(site->wells, "wells");
+    ONEKA_CHECK_ARG(out->coef && out->q && out->aquifer, "out->coef/q/aquifer");
+    ONEKA_CHECK_ARG(mode == ONEKA_MODE_GIVEN || mode == ONEKA_MODE_GIVEN_EV || qdist, "qdist");
+    for (int a = 0; a < 3; ++a)
+        ONEKA_CHECK_ARG(adist[a].kind >= ONEKA_DIST_CONST && adist[a].kind <= ONEKA_DIST_LOGNORMAL,
+                        "adist kind");
+    ONEKA_CHECK_CUDA(launch_realize(*site, qdist, adist, logr2, seed, first, nreal, mode, *out,
+                                    (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+size_t oneka_track_scratch_bytes(const OnekaGrid* grid, int32_t slots) {
+    if (!grid_ok(grid) || slots < 0) return 0;
+    return (size_t)slot_words(*grid) * 4u * (size_t)slots;
+}
+
+int oneka_track(const OnekaSite* site, const OnekaRealizations* real, int32_t nreal,
+                const double* release, int32_t npaths, const OnekaTrackOpts* opts,
+                const OnekaGrid* grid, const OnekaFrame* frames, int32_t* counts,
+                int64_t* registered, const OnekaTrackOut* out, void* scratch,
+                size_t scratch_bytes, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(site && real && opts && grid, "site/real/opts/grid");
+    ONEKA_CHECK_ARG(grid_ok(grid), "grid (nrows, ncols, dx, dy must be > 0)");
+    ONEKA_CHECK_ARG(nreal >= 0 && npaths >= 0, "nreal/npaths");
+    ONEKA_CHECK_ARG(npaths == 0 || release, "release");
+    ONEKA_CHECK_ARG(site->nwells >= 1 && site->nwells <= 2048 && site->wells, "wells (1..2048)");
+    ONEKA_CHECK_ARG(site->target >= 0 && site->target < site->nwells, "target index");
+    ONEKA_CHECK_ARG(real->coef && real->q && real->aquifer, "realization arrays");
+    ONEKA_CHECK_ARG(opts->precision == ONEKA_FP64 || opts->precision == ONEKA_FP32, "precision");
+    ONEKA_CHECK_ARG(opts->tol > 0 && opts->maxstep > 0 && opts->umbra >= 0, "tol/maxstep/umbra");
+    ONEKA_CHECK_ARG(opts->block == 0 || (opts->block % 32 == 0 && opts->block <= 256), "block");
+    ONEKA_CHECK_ARG(!out || out->max_vertices >= 0, "max_vertices");
+    ONEKA_CHECK_ARG(!out || !out->vertices || out->max_vertices > 0, "vertices without max_vertices");
+    if (nreal == 0) return ONEKA_OK;
+
+    cudaStream_t s = (cudaStream_t)stream;
+    TrackLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.nwells = site->nwells;
+    L.npaths = npaths;
+    L.wells = site->wells;
+    L.xo = site->xo;
+    L.yo = site->yo;
+    // The regional origin anchors the FP32 build's relative coordinates (the
+    // stochastic driver puts it on the target well).
+    L.xt = site->xo;
+    L.yt = site->yo;
+    L.coef = real->coef;
+    L.q = real->q;
+    L.aquifer = real->aquifer;
+    L.rstatus = real->status;
+    L.release = release;
+    L.opts = *opts;
+    L.grid = *grid;
+    L.frames = frames;
+    L.wpr = words_per_row(grid->ncols);
+    L.slot_words = slot_words(*grid);
+    L.mask_words = mask_words(*grid);
+    L.registered = (unsigned long long*)registered;
+    if (out) L.out = *out;
+    L.max_attempts = opts->max_attempts > 0 ? opts->max_attempts : kDefaultMaxAttempts;
+
+    int wave = nreal < 65535 ? nreal : 65535;
+    if (!counts && scratch) {
+        // mark-only: realization k ORs its traces into slot k of scratch; no
+        // clearing and no register (the caller registers, e.g. with weights)
+        const size_t need = (size_t)L.slot_words * 4u * (size_t)nreal;
+        if (scratch_bytes < need) {
+            set_error("mark-only scratch of %zu bytes is smaller than %d slots (%zu bytes)",
+                      scratch_bytes, nreal, need);
+            return ONEKA_ERR_SCRATCH;
+        }
+        ONEKA_CHECK_ARG(((uintptr_t)scratch & 15u) == 0, "scratch must be 16-byte aligned");
+        L.slots = (uint32_t*)scratch;
+        for (int r0 = 0; r0 < nreal; r0 += wave) {
+            L.r0 = r0;
+            L.nr = (nreal - r0) < wave ? (nreal - r0) : wave;
+            TrackLaunch Lw = L;
+            Lw.slots = L.slots + (long long)r0 * L.slot_words;
+            ONEKA_CHECK_CUDA(opts->precision == ONEKA_FP64 ? launch_track64(Lw, s) : launch_track32(Lw, s));
+        }
+        return ONEKA_OK;
+    }
+    if (counts) {
+        const size_t slot_bytes = (size_t)L.slot_words * 4u;
+        ONEKA_CHECK_ARG(scratch != nullptr, "scratch is required when counts is given");
+        if (scratch_bytes < slot_bytes) {
+            set_error("scratch of %zu bytes is smaller than one realization slot (%zu bytes)",
+                      scratch_bytes, slot_bytes);
+            return ONEKA_ERR_SCRATCH;
+        }
+        ONEKA_CHECK_ARG(((uintptr_t)scratch & 15u) == 0, "scratch must be 16-byte aligned");
+        const size_t fit = scratch_bytes / slot_bytes;
+        if ((size_t)wave > fit) wave = (int)fit;
+        L.slots = (uint32_t*)scratch;
+    }
+    for (int r0 = 0; r0 < nreal; r0 += wave) {
+        L.r0 = r0;
+        L.nr = (nreal - r0) < wave ? (nreal - r0) : wave;
+        ONEKA_CHECK_CUDA(opts->precision == ONEKA_FP64 ? launch_track64(L, s) : launch_track32(L, s));
+        if (counts) ONEKA_CHECK_CUDA(launch_register_counts(L.slots, L.nr, *grid, counts, s));
+    }
+    return ONEKA_OK;
+}
+
+int oneka_evaluate(const OnekaSite* site, const double* q, double conductivity, double porosity,
+                   double thickness, const double* coef, const double* points, int64_t npts,
+                   int32_t confined, double* potential, double* discharge, double* head,
+                   double* velocity, int32_t* status, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(site && coef && (npts == 0 || points), "site/coef/points");
+    ONEKA_CHECK_ARG(site->nwells >= 0 && (site->nwells == 0 || (site->wells && q)), "wells/q");
+    ONEKA_CHECK_ARG(npts >= 0, "npts");
+    ONEKA_CHECK_CUDA(launch_evaluate(*site, q, conductivity, porosity, thickness, coef, points, npts,
+                                     confined, potential, discharge, head, velocity, status,
+                                     (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_rasterize(const OnekaGrid* grid, const OnekaFrame* frame, const double* xy, int64_t n,
+                    double umbra, uint32_t* mask, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(grid_ok(grid) && mask && n >= 0 && (n == 0 || xy), "grid/mask/xy");
+    ONEKA_CHECK_ARG(umbra >= 0, "umbra");
+    OnekaFrame f;
+    if (frame) {
+        f = *frame;
+    } else {
+        f.xmin = grid->xmin;
+        f.ymin = grid->ymin;
+        f.coff = f.roff = 0;
+        f.ncols = grid->ncols;
+        f.nrows = grid->nrows;
+    }
+    ONEKA_CHECK_CUDA(launch_rasterize(*grid, f, xy, n, umbra, mask, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_register_weighted(const OnekaGrid* grid, uint32_t* mask, double weight, double* pgrid,
+                            void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(grid_ok(grid) && mask && pgrid, "grid/mask/pgrid");
+    ONEKA_CHECK_CUDA(launch_register_weighted(mask, *grid, weight, pgrid, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_fma_peak(int32_t fp64, double* flops_per_s, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(flops_per_s, "flops_per_s");
+    ONEKA_CHECK_CUDA(probe_fma(fp64, flops_per_s, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_distancesquared(const double* abc, double* d2, int64_t n, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(n >= 0 && (n == 0 || (abc && d2)), "abc/d2");
+    ONEKA_CHECK_CUDA(launch_distancesquared(abc, d2, n, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+}  // extern "C"

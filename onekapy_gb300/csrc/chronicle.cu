@@ -1,0 +1,212 @@
+// chronicle.cu -- ProbabilityField kernels and pointwise model evaluation (FP64).
+//
+// Built with --fmad=false (reference FP64 arithmetic).  References (paths
+// within OnekaPy):
+//   oneka/probabilityfield.py:313-339   rasterize / insert      -> rasterize_kernel
+//   oneka/probabilityfield.py:342-372   register / reset        -> register_*_kernel
+//   oneka/probabilityfield.py:380-427   distancesquared         -> distancesquared_kernel
+//   oneka/model.py:207-427              potential .. velocity   -> evaluate_kernel
+#include <math.h>
+
+#include "oneka_internal.cuh"
+
+namespace oneka {
+namespace {
+
+// One block per realization slot: scan the rows its particles touched (the
+// slot header), add 1 to counts for every marked node, and clear the words
+// and the header as they are read (register() then rgrid[:] = False).
+__global__ void __launch_bounds__(256) register_counts_kernel(uint32_t* __restrict__ slots,
+                                                              long long slot_words, long long mask_words,
+                                                              int nrows, int ncols, int wpr,
+                                                              int32_t* __restrict__ counts) {
+    uint32_t* slot = slots + (long long)blockIdx.x * slot_words;
+    const uint32_t h0 = slot[mask_words], h1 = slot[mask_words + 1];
+    if (h1 == 0) return;
+    // the header is written only by the tracker; clamping keeps a corrupted
+    // header from leading the scan outside the slot
+    const int rlo = h0 > (uint32_t)nrows ? 0 : nrows - (int)h0;
+    const int rhi = h1 > (uint32_t)nrows ? nrows - 1 : (int)h1 - 1;
+    const long long w0 = (long long)rlo * wpr, w1 = (long long)(rhi + 1) * wpr;
+    for (long long w = w0 + threadIdx.x; w < w1; w += blockDim.x) {
+        uint32_t v = slot[w];
+        if (!v) continue;
+        slot[w] = 0u;
+        const int row = (int)(w / wpr);
+        const int col0 = (int)(w % wpr) * 32;
+        int32_t* crow = counts + (long long)row * ncols + col0;
+        while (v) {
+            const int b = __ffs(v) - 1;
+            v &= v - 1;
+            atomicAdd(crow + b, 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        slot[mask_words] = 0u;
+        slot[mask_words + 1] = 0u;
+    }
+}
+
+__global__ void register_weighted_kernel(uint32_t* __restrict__ mask, long long mwords, int nrows, int ncols,
+                                         int wpr, double weight, double* __restrict__ pgrid) {
+    const long long word = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (word >= (long long)nrows * wpr) return;
+    const uint32_t w = mask[word];
+    const int row = (int)(word / wpr);
+    const int col = (int)(word % wpr) * 32 + lane;
+    if (((w >> lane) & 1u) && col < ncols) {
+        double* cell = pgrid + (long long)row * ncols + col;
+        *cell = *cell + weight;
+    }
+    __syncwarp();
+    if (lane == 0) mask[word] = 0u;
+    if (word == 0 && lane < 4) mask[mwords + lane] = 0u;
+}
+
+__global__ void rasterize_kernel(OnekaGrid g, OnekaFrame f, const double* __restrict__ xy, long long n,
+                                 double umbra, uint32_t* mask, int wpr) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + 1 >= n) return;
+    long long ntest = 0, natom = 0;
+    int rlo = 0x7fffffff, rhi = -1;
+    insert64(mask, wpr, g.nrows, g.ncols, f, g.dx, g.dy, umbra, xy[2 * i], xy[2 * i + 1],
+             xy[2 * i + 2], xy[2 * i + 3], ntest, natom, rlo, rhi);
+}
+
+__global__ void distancesquared_kernel(const double* __restrict__ abc, double* __restrict__ d2, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = abc + 6 * i;
+    const double bax = a[2] - a[0];
+    const double bay = a[3] - a[1];
+    const double cax = a[4] - a[0];
+    const double cay = a[5] - a[1];
+    const double perpdot = bax * cay - bay * cax;
+    const double dot = bax * cax + bay * cay;
+    const double length2 = bax * bax + bay * bay;
+    const double alpha2 = perpdot * perpdot / length2;
+    const double beta2 = dot * dot / length2;
+    double r;
+    if (dot < 0) r = alpha2 + beta2;
+    else if (beta2 > length2) r = alpha2 + beta2 - 2 * dot + length2;
+    else r = alpha2;
+    d2[i] = r;
+}
+
+struct EvalModel {
+    const double* wells;   // [nw][3]
+    const double* q;       // [nw]
+    int nw;
+    double xo, yo, c[6], K, n, H;
+};
+
+__global__ void evaluate_kernel(EvalModel m, const double* __restrict__ pts, long long npts, int confined,
+                                double* potential, double* discharge, double* head, double* velocity,
+                                int32_t* status) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npts) return;
+    const double x = pts[2 * i], y = pts[2 * i + 1];
+    // compute_discharge (model.py:299-315)
+    double dx = x - m.xo, dy = y - m.yo;
+    double Qx = -(2.0 * m.c[0] * dx + m.c[2] * dy + m.c[3]);
+    double Qy = -(2.0 * m.c[1] * dy + m.c[2] * dx + m.c[4]);
+    // compute_potential (model.py:225-237)
+    double pot = (m.c[0] * (dx * dx) + m.c[1] * (dy * dy) + m.c[2] * dx * dy + m.c[3] * dx + m.c[4] * dy + m.c[5]);
+    double pw = 0.0;
+    for (int w = 0; w < m.nw; ++w) {
+        const double ddx = x - m.wells[3 * w], ddy = y - m.wells[3 * w + 1];
+        const double r2 = ddx * ddx + ddy * ddy;
+        Qx += -m.q[w] * ddx / r2 * 0.15915494309189535;
+        Qy += -m.q[w] * ddy / r2 * 0.15915494309189535;
+        pw += m.q[w] * log(r2) * 0.07957747154594767;
+    }
+    pot += pw;
+    // compute_head (model.py:341-350)
+    int st = ONEKA_TRACE_OK;
+    double h = NAN;
+    if (pot <= 0) {
+        st = ONEKA_TRACE_DRY;
+    } else {
+        const double kh2 = 0.5 * m.K * (m.H * m.H);
+        h = (pot < kh2) ? sqrt(2.0 * pot / m.K) : (pot + kh2) / (m.K * m.H);
+    }
+    // compute_velocity / compute_velocity_confined (model.py:377-389, 423-427)
+    double vx = NAN, vy = NAN;
+    if (confined) {
+        vx = Qx / (m.H * m.n);
+        vy = Qy / (m.H * m.n);
+    } else if (st == ONEKA_TRACE_OK) {
+        if (h <= 0) {
+            st = ONEKA_TRACE_DRY;
+        } else if (h > m.H) {
+            vx = Qx / (m.H * m.n);
+            vy = Qy / (m.H * m.n);
+        } else {
+            vx = Qx / (h * m.n);
+            vy = Qy / (h * m.n);
+        }
+    }
+    if (potential) potential[i] = pot;
+    if (discharge) { discharge[2 * i] = Qx; discharge[2 * i + 1] = Qy; }
+    if (head) head[i] = h;
+    if (velocity) { velocity[2 * i] = vx; velocity[2 * i + 1] = vy; }
+    if (status) status[i] = confined ? ONEKA_TRACE_OK : st;
+}
+
+unsigned blocks_for(long long n, int per_block) { return (unsigned)((n + per_block - 1) / per_block); }
+
+}  // namespace
+
+cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid& g, int32_t* counts,
+                                   cudaStream_t s) {
+    if (nslots <= 0) return cudaSuccess;
+    register_counts_kernel<<<(unsigned)nslots, 256, 0, s>>>(slots, slot_words(g), mask_words(g), g.nrows,
+                                                            g.ncols, words_per_row(g.ncols), counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_register_weighted(uint32_t* mask, const OnekaGrid& g, double weight, double* pgrid,
+                                     cudaStream_t s) {
+    const int wpr = words_per_row(g.ncols);
+    const long long words = (long long)g.nrows * wpr;
+    register_weighted_kernel<<<blocks_for(words, 8), 256, 0, s>>>(mask, mask_words(g), g.nrows, g.ncols, wpr,
+                                                                  weight, pgrid);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rasterize(const OnekaGrid& g, const OnekaFrame& f, const double* xy, long long n,
+                             double umbra, uint32_t* mask, cudaStream_t s) {
+    if (n < 2) return cudaSuccess;
+    rasterize_kernel<<<blocks_for(n - 1, 128), 128, 0, s>>>(g, f, xy, n, umbra, mask, words_per_row(g.ncols));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_distancesquared(const double* abc, double* d2, long long n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    distancesquared_kernel<<<blocks_for(n, 256), 256, 0, s>>>(abc, d2, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evaluate(const OnekaSite& site, const double* q, double K, double n, double H,
+                            const double* coef, const double* pts, long long npts, int confined,
+                            double* potential, double* discharge, double* head, double* velocity,
+                            int32_t* status, cudaStream_t s) {
+    if (npts <= 0) return cudaSuccess;
+    EvalModel m;
+    m.wells = site.wells;
+    m.q = q;
+    m.nw = site.nwells;
+    m.xo = site.xo;
+    m.yo = site.yo;
+    for (int i = 0; i < 6; ++i) m.c[i] = coef[i];
+    m.K = K;
+    m.n = n;
+    m.H = H;
+    evaluate_kernel<<<blocks_for(npts, 128), 128, 0, s>>>(m, pts, npts, confined, potential, discharge,
+                                                          head, velocity, status);
+    return cudaGetLastError();
+}
+
+}  // namespace oneka

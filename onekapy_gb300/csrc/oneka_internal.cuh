@@ -1,0 +1,197 @@
+// oneka_internal.cuh -- shared declarations of liboneka_gb300 (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/oneka_gb300.h"
+
+namespace oneka {
+
+constexpr int kTraceSkipped = 3;              // per-particle status of an untracked realization
+constexpr int kDefaultMaxAttempts = 1000000;
+
+// Everything one tracking launch needs, passed by value as the kernel parameter.
+struct TrackLaunch {
+    const double* wells;        // [nwells][3]
+    int nwells;
+    int npaths;
+    double xo, yo;              // regional origin
+    double xt, yt;              // target well (FP32 build: coordinates relative to it)
+    const double* coef;         // [nreal][6]
+    const double* q;            // [nreal][nwells]
+    const double* aquifer;      // [nreal][3]
+    const int32_t* rstatus;     // [nreal] or null
+    int r0;                     // first realization of this wave
+    int nr;                     // realizations in this wave
+    const double* release;      // [npaths][2]
+    OnekaTrackOpts opts;
+    OnekaGrid grid;
+    const OnekaFrame* frames;   // [nreal][npaths] or null
+    uint32_t* slots;            // wave-local realization k uses slots + k * slot_words; null: no chronicle
+    int wpr;                    // words per grid row
+    long long slot_words;
+    long long mask_words;
+    unsigned long long* registered;
+    OnekaTrackOut out;
+    int max_attempts;
+};
+
+// A realization slot: the bitmask (nrows rows of words_per_row words), padded
+// to a multiple of 4 words, then a 4-word header { h0, h1, 0, 0 } recording
+// the rows touched: h0 = max(nrows - row), h1 = max(row + 1) over marked
+// rows, so an all-zero slot is an empty one.
+inline int words_per_row(int ncols) { return (ncols + 31) / 32; }
+inline long long mask_words(const OnekaGrid& g) {
+    long long w = (long long)g.nrows * words_per_row(g.ncols);
+    return (w + 3) / 4 * 4;
+}
+inline long long slot_words(const OnekaGrid& g) { return mask_words(g) + 4; }
+
+cudaError_t launch_track64(const TrackLaunch& L, cudaStream_t s);
+cudaError_t launch_track32(const TrackLaunch& L, cudaStream_t s);
+cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid& g, int32_t* counts,
+                                   cudaStream_t s);
+
+void set_error(const char* fmt, ...);
+
+// Dormand-Prince 5(4) tableau (capturezone.py:202-209); every entry is the
+// double nearest the rational, as Python's true division gives.
+struct DP {
+    static constexpr double a2 = 1.0 / 5.0;
+    static constexpr double a31 = 3.0 / 40.0, a32 = 9.0 / 40.0;
+    static constexpr double a41 = 44.0 / 45.0, a42 = -56.0 / 15.0, a43 = 32.0 / 9.0;
+    static constexpr double a51 = 19372.0 / 6561.0, a52 = -25360.0 / 2187.0,
+                            a53 = 64448.0 / 6561.0, a54 = -212.0 / 729.0;
+    static constexpr double a61 = 9017.0 / 3168.0, a62 = -355.0 / 33.0, a63 = 46732.0 / 5247.0,
+                            a64 = 49.0 / 176.0, a65 = -5103.0 / 18656.0;
+    static constexpr double a71 = 35.0 / 384.0, a73 = 500.0 / 1113.0, a74 = 125.0 / 192.0,
+                            a75 = -2187.0 / 6784.0, a76 = 11.0 / 84.0;
+    static constexpr double e1 = 71.0 / 57600.0, e2 = -1.0 / 40.0, e3 = -71.0 / 16695.0,
+                            e4 = 71.0 / 1920.0, e5 = -17253.0 / 339200.0, e6 = 22.0 / 525.0;
+    static constexpr double eps = 2.220446049250313e-16;   // np.finfo(float).eps
+};
+
+// Python's min(a, b): the first argument unless the second is strictly smaller.
+__device__ __forceinline__ double py_min(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double py_max(double a, double b) { return (b > a) ? b : a; }
+
+// The frame a particle's trace is rasterized against.
+__device__ __forceinline__ OnekaFrame frame_of(const TrackLaunch& L, int r, int p) {
+    if (L.frames) return L.frames[(long long)r * L.npaths + p];
+    OnekaFrame f;
+    f.xmin = L.grid.xmin;
+    f.ymin = L.grid.ymin;
+    f.coff = 0;
+    f.roff = 0;
+    f.ncols = L.grid.ncols;
+    f.nrows = L.grid.nrows;
+    return f;
+}
+
+// Clamp floor() results (as doubles) to a half-open index range [0, n).
+__device__ __forceinline__ bool clip_range(double lo, double hi, int n, int& ilo, int& ihi) {
+    if (!(lo < (double)n) || !(hi > 0.0)) return false;
+    ilo = lo < 0.0 ? 0 : (int)lo;
+    ihi = hi > (double)n ? n : (int)hi;
+    return ilo < ihi;
+}
+
+// ProbabilityField.distancesquared(...) < umbra**2 with the reference's FP64
+// operations (probabilityfield.py:407-427).  A reciprocal replaces the two
+// divisions unless the result lies within 1e-12 (relative) of the threshold,
+// where the exact quotients decide; the outcome equals the reference's.
+__device__ __forceinline__ bool in_umbra64(double bax, double bay, double cax, double cay,
+                                           double length2, double inv, bool fast_ok, double u2) {
+    const double perpdot = bax * cay - bay * cax;
+    const double dot = bax * cax + bay * cay;
+    if (fast_ok) {
+        const double a2 = perpdot * perpdot * inv;
+        const double b2 = dot * dot * inv;
+        double d2;
+        if (dot < 0) d2 = a2 + b2;
+        else if (b2 > length2) d2 = a2 + b2 - 2 * dot + length2;
+        else d2 = a2;
+        const double margin = 1e-12 * (a2 + b2 + 2 * fabs(dot) + length2 + u2);
+        if (d2 < u2 - margin) return true;
+        if (d2 > u2 + margin) return false;
+    }
+    const double alpha2 = perpdot * perpdot / length2;
+    const double beta2 = dot * dot / length2;
+    double d2;
+    if (dot < 0) d2 = alpha2 + beta2;
+    else if (beta2 > length2) d2 = alpha2 + beta2 - 2 * dot + length2;
+    else d2 = alpha2;
+    return d2 < u2;
+}
+
+// ProbabilityField.insert (probabilityfield.py:296-310) into a realization
+// bitmask: every node of the frame within umbra of segment a-b is OR-ed in,
+// one atomicOr per touched 32-node word of a row.
+__device__ __forceinline__ void insert64(uint32_t* __restrict__ slot, int wpr, int gnrows, int gncols,
+                                         const OnekaFrame& f, double dx, double dy, double umbra,
+                                         double ax, double ay, double bx, double by,
+                                         long long& ntest, long long& natom, int& rlo, int& rhi) {
+    const double u2 = umbra * umbra;
+    int left, right, bottom, top;
+    if (!clip_range(floor((py_min(ax, bx) - umbra - f.xmin) / dx),
+                    floor((py_max(ax, bx) + umbra - f.xmin) / dx) + 1, f.ncols, left, right))
+        return;
+    if (!clip_range(floor((py_min(ay, by) - umbra - f.ymin) / dy),
+                    floor((py_max(ay, by) + umbra - f.ymin) / dy) + 1, f.nrows, bottom, top))
+        return;
+    ntest += (long long)(right - left) * (top - bottom);
+    const double bax = bx - ax;
+    const double bay = by - ay;
+    const double length2 = bax * bax + bay * bay;
+    const double inv = 1.0 / length2;
+    const bool fast_ok = (length2 > 1e-250) && (inv < 1e250);
+    for (int i = bottom; i < top; ++i) {
+        const int gi = i + f.roff;
+        if (gi < 0 || gi >= gnrows) continue;
+        const double cy = f.ymin + (double)i * dy;
+        const double cay = cy - ay;
+        uint32_t acc = 0;
+        int curw = -1;
+        uint32_t* row = slot + (long long)gi * wpr;
+        for (int j = left; j < right; ++j) {
+            const int gj = j + f.coff;
+            if (gj < 0 || gj >= gncols) continue;
+            const double cx = f.xmin + (double)j * dx;
+            const double cax = cx - ax;
+            if (in_umbra64(bax, bay, cax, cay, length2, inv, fast_ok, u2)) {
+                const int w = gj >> 5;
+                if (w != curw) {
+                    if (acc) { atomicOr(row + curw, acc); ++natom; }
+                    curw = w;
+                    acc = 0;
+                }
+                acc |= 1u << (gj & 31);
+            }
+        }
+        if (curw >= 0) {
+            if (acc) { atomicOr(row + curw, acc); ++natom; }
+            rlo = gi < rlo ? gi : rlo;
+            rhi = gi > rhi ? gi : rhi;
+        }
+    }
+}
+
+// Record the rows a particle marked in its slot's header (see slot_words).
+__device__ __forceinline__ void note_rows(uint32_t* slot, long long mwords, int nrows, int rlo, int rhi) {
+    if (!slot || rhi < rlo) return;
+    atomicMax(slot + mwords, (uint32_t)(nrows - rlo));
+    atomicMax(slot + mwords + 1, (uint32_t)(rhi + 1));
+}
+
+// Per-thread work counters, added into OnekaTrackOut.counters at the end.
+__device__ __forceinline__ void add_counters(long long* c, long long att, long long acc, long long ntest,
+                                             long long natom) {
+    if (!c) return;
+    atomicAdd((unsigned long long*)c + 0, (unsigned long long)att);
+    atomicAdd((unsigned long long*)c + 1, (unsigned long long)acc);
+    atomicAdd((unsigned long long*)c + 2, (unsigned long long)ntest);
+    atomicAdd((unsigned long long*)c + 3, (unsigned long long)natom);
+}
+
+}  // namespace oneka

@@ -1,0 +1,135 @@
+"""CPU-only checks: the C ABI library loads and exports every declared symbol,
+the ctypes structs match the header's layout, and the host-side logic."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, TRACK_CASES, golden
+
+HEADER = os.path.join(ROOT, "include", "oneka_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from onekapy_gb300 import build
+    build.build()
+    from onekapy_gb300 import _capi
+    return _capi.load()
+
+
+def _declared():
+    src = open(HEADER).read()
+    return re.findall(r"ONEKA_API\s+[\w\s\*]*?\b(oneka_\w+)\s*\(", src)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+    from onekapy_gb300 import _capi
+    assert set(_capi.EXPORTS) <= set(names)
+
+
+def test_abi_version_and_error_string(lib):
+    assert lib.oneka_abi_version() == 1
+    assert lib.oneka_last_error() == b""
+
+
+def test_invalid_arguments_return_error_without_gpu(lib):
+    from onekapy_gb300 import _capi as C
+    rc = lib.oneka_distancesquared(None, None, -1, None)
+    assert rc == C.ONEKA_ERR_INVALID
+    assert b"invalid argument" in lib.oneka_last_error()
+    g = C.OnekaGrid(0.0, 0.0, 0.0, 1.0, 3, 3)
+    assert lib.oneka_track_scratch_bytes(ctypes.byref(g), 1) == 0
+    g = C.OnekaGrid(0.0, 0.0, 5.0, 5.0, 1601, 1601)
+    assert lib.oneka_track_scratch_bytes(ctypes.byref(g), 1) == 4 * ((1601 * 51 + 3) // 4 * 4 + 4)
+
+
+def test_struct_layout_matches_header():
+    """Compile a probe against the header and compare sizes/offsets with ctypes."""
+    from onekapy_gb300 import _capi as C
+    structs = ["OnekaDist", "OnekaSite", "OnekaRealizations", "OnekaGrid", "OnekaFrame",
+               "OnekaTrackOpts", "OnekaTrackOut"]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){"]
+    for s in structs:
+        lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
+        for fname, _ in getattr(C, s)._fields_:
+            lines.append(f'printf("{s}.{fname} %zu\\n", offsetof({s}, {fname}));')
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as td:
+        src = os.path.join(td, "probe.c")
+        exe = os.path.join(td, "probe")
+        open(src, "w").write("\n".join(lines))
+        subprocess.run(["gcc", "-o", exe, src], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    got = dict(line.split() for line in out.strip().splitlines())
+    for s in structs:
+        cls = getattr(C, s)
+        assert int(got[s]) == ctypes.sizeof(cls), s
+        for fname, _ in cls._fields_:
+            assert int(got[f"{s}.{fname}"]) == getattr(cls, fname).offset, f"{s}.{fname}"
+
+
+def test_replay_expand_matches_oracle_sequential(oracle_mod):
+    from onekapy_gb300 import engine as E
+    rng = np.random.default_rng(0)
+    for trial in range(100):
+        dx = [1.0, 2.5, 0.7, 10.0, 3.3][trial % 5]
+        xo, yo = rng.uniform(-1000, 1000, 2)
+        n = int(rng.integers(1, 30))
+        c = rng.uniform(-50, 50, (n, 2)) + [xo, yo]
+        w = rng.uniform(0, 40, (n, 2))
+        bb = np.stack([c[:, 0] - w[:, 0], c[:, 0] + w[:, 0], c[:, 1] - w[:, 1], c[:, 1] + w[:, 1]], 1)
+        if trial % 7 == 0:
+            bb = np.round(bb / dx) * dx
+        a = oracle_mod.replay_expand(xo, yo, dx, dx, bb)
+        b = E.replay_expand(xo, yo, dx, dx, bb)
+        assert a[0] == b[0]
+        for k in a[1].dtype.names:
+            assert np.array_equal(a[1][k], b[1][k]), (trial, k)
+
+
+@pytest.mark.parametrize("case", TRACK_CASES)
+def test_window_and_release_match_reference(case):
+    from onekapy_gb300 import engine as E
+    d = golden(f"track_{case}.npz")
+    xt, yt, rt = d["wells"][0]
+    g = d["grid"]
+    half = (g[5] - 1) * g[2] / 2
+    grid = E.Grid.window(xt, yt, float(d["spacing"]), half)
+    assert (grid.xmin, grid.ymin, grid.nrows, grid.ncols) == (g[0], g[1], int(g[4]), int(g[5]))
+    assert np.array_equal(E.release_ring(xt, yt, rt, int(d["npaths"])), d["release"])
+
+
+def test_distribution_helpers():
+    from onekapy_gb300 import engine as E
+    from onekapy_gb300 import stochastic as St
+    assert E.dist(5).kind == 0 and E.dist((1, 2)).kind == 1 and E.dist((1, 2, 3)).kind == 2
+    assert E.dist(E.Lognormal(1.0, 0.5)).kind == 3
+    with pytest.raises(E.DistributionError):
+        E.dist((1, 2, 3, 4))
+    assert St.compute_variate_mean((1.0, 3.0)) == 2.0
+    assert St.compute_variate_mean((1.0, 2.0, 6.0)) == 3.0
+    assert St.isdistribution((0.1, 0.2), 0, 1) and not St.isdistribution((0.3, 0.2), 0, 1)
+    np.random.seed(0)
+    v = St.generate_random_variate((10.0, 20.0))
+    assert 10.0 <= v <= 20.0
+
+
+def test_synthetic_sites_have_the_configured_shapes():
+    from onekapy_gb300 import sites as S
+    c1, c2, c4 = S.config1(), S.config2(), S.config4()
+    assert (len(c1.wells), len(c1.observations), c1.nreal, c1.npaths) == (4, 25, 100, 100)
+    assert (len(c2.wells), len(c2.observations), c2.nreal, c2.npaths) == (11, 60, 10000, 1000)
+    assert (len(c4.wells), c4.nreal, c4.npaths) == (31, 5000, 2048)
+    c3 = S.config3()
+    assert len(c3) == 64
+    assert all(2 <= len(s.wells) - 1 <= 200 and 20 <= len(s.observations) <= 200 for s in c3)
+    assert S.config1().observations == c1.observations   # seeded

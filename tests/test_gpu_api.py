@@ -1,0 +1,164 @@
+"""GPU: the reference-compatible API and full-size workloads against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+from onekapy_gb300 import _capi as C  # noqa: E402
+from onekapy_gb300 import engine as E  # noqa: E402
+from onekapy_gb300 import sites as S  # noqa: E402
+
+
+def _oracle_counts(oracle_mod, site, real, spec, grid, frames=None, nthreads=0):
+    wells = site.wells.cpu().numpy()[:, :2]
+    return oracle_mod.track(wells, real.coef.cpu().numpy(), real.q.cpu().numpy(),
+                            real.aquifer.cpu().numpy(), site.release(spec.npaths),
+                            (grid.xmin, grid.ymin, grid.dx, grid.dy, grid.nrows, grid.ncols),
+                            duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep,
+                            umbra=spec.umbra, confined=spec.confined, base=spec.base,
+                            xo=site.xo, yo=site.yo, frames=frames, nthreads=nthreads)
+
+
+def _gpu_counts(site, real, spec, grid, precision, outputs=None):
+    dev = site.device
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+    reg = torch.zeros(1, dtype=torch.int64, device=dev)
+    opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=spec.confined, precision=precision)
+    E.track(site, real, torch.as_tensor(site.release(spec.npaths), device=dev), opts, grid,
+            counts=counts, registered=reg, outputs=outputs)
+    torch.cuda.synchronize()
+    return counts.cpu().numpy(), int(reg.item())
+
+
+def _site(spec):
+    return E.Site(spec.wells, spec.observations, spec.base, target=spec.target, c_dist=spec.c_dist,
+                  p_dist=spec.p_dist, t_dist=spec.t_dist, device=C.device())
+
+
+def test_compute_backtrace_matches_reference():
+    from onekapy_gb300.capturezone import compute_backtrace
+    from onekapy_gb300.model import Model, make_feval
+    d = golden("backtrace_cases.npz")
+    mo = Model(0.0, 10.0, 0.25, 25.0, [(0.0, 0.0, 0.25, 500.0), (300.0, -200.0, 0.25, 200.0)],
+               0.0, 0.0, d["coef"])
+    feval = make_feval(mo, confined=True)
+    for k, (xs, ys, dur) in enumerate(d["starts"]):
+        v = np.array(compute_backtrace(xs, ys, dur, 1, 5, feval))
+        n = int(d["nvertices"][k])
+        assert v.shape == (n, 2)
+        assert np.allclose(v, d["vertices"][k, :n], rtol=1e-12, atol=1e-9)
+
+
+def test_compute_backtrace_rejects_python_feval():
+    from onekapy_gb300.capturezone import compute_backtrace
+    with pytest.raises(TypeError):
+        compute_backtrace(0.0, 0.0, 10.0, 1, 5, lambda xy: np.zeros(2))
+
+
+def test_compute_capturezone_dropin_on_growing_grid():
+    """ProbabilityField starting at 3x3 around the target grows as in the reference."""
+    from onekapy_gb300.capturezone import compute_capturezone
+    from onekapy_gb300.model import Model, make_feval
+    from onekapy_gb300.probabilityfield import ProbabilityField
+    d = golden("track_expanding_u20.npz")
+    xt, yt, rt = d["wells"][0]
+    pf = ProbabilityField(float(d["spacing"]), float(d["spacing"]), xt, yt)
+    for r in range(d["coef"].shape[0]):
+        wl = [(w[0], w[1], w[2], q) for w, q in zip(d["wells"], d["q"][r])]
+        mo = Model(float(d["base"]), d["K"][r], d["n"][r], d["H"][r], wl, xt, yt, d["coef"][r])
+        compute_capturezone(xt, yt, rt, int(d["npaths"]), float(d["duration"]), pf, float(d["umbra"]),
+                            1.0, float(d["tol"]), float(d["maxstep"]), make_feval(mo, bool(d["confined"])))
+    assert (pf.xmin, pf.ymin, pf.nrows, pf.ncols) == (d["grid"][0], d["grid"][1], d["grid"][4], d["grid"][5])
+    assert pf.total_weight == d["total_weight"]
+    assert np.array_equal(pf.pgrid.cpu().numpy(), d["counts"].astype(np.float64))
+
+
+def test_config1_full_fp64_bit_exact_vs_oracle(oracle_mod):
+    """Config 1 in full (100 realizations x 100 paths) on the fixed 4 km window."""
+    spec = S.config1()
+    site = _site(spec)
+    real = E.realize(site, spec.nreal, seed=1001)
+    assert int((real.status != 0).sum()) == 0
+    grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+    got, reg = _gpu_counts(site, real, spec, grid, C.FP64)
+    want = _oracle_counts(oracle_mod, site, real, spec, grid)
+    assert reg == spec.nreal == want["registered"]
+    assert np.array_equal(got, want["counts"]), f"{(got != want['counts']).sum()} nodes differ"
+    got32, _ = _gpu_counts(site, real, spec, grid, C.FP32)
+    linf = np.abs(got32 - got).max() / spec.nreal
+    assert linf <= 0.01, linf
+
+
+def test_config2_subset_fp64_bit_exact_vs_oracle(oracle_mod):
+    """Config 2 site (mixed aquifer, general head path), 24 realizations x 200 paths."""
+    spec = S.config2(nreal=24, npaths=200)
+    site = _site(spec)
+    real = E.realize(site, spec.nreal, seed=1002)
+    grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+    out = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
+    got, reg = _gpu_counts(site, real, spec, grid, C.FP64, outputs=out)
+    want = _oracle_counts(oracle_mod, site, real, spec, grid)
+    assert reg == want["registered"]
+    assert np.array_equal(out.naccept.cpu().numpy(), want["naccept"])
+    assert np.array_equal(got, want["counts"]), f"{(got != want['counts']).sum()} nodes differ"
+
+
+def test_config4_subset_fp64_vs_oracle_and_fp32(oracle_mod):
+    """Config 4 (thin unconfined, 31 wells): FP64 parity and the FP32 precision split."""
+    spec = S.config4(nreal=12, npaths=128)
+    site = _site(spec)
+    real = E.realize(site, spec.nreal, seed=1004)
+    ok = real.status.cpu().numpy() == 0
+    grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+    out64 = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
+    got, reg = _gpu_counts(site, real, spec, grid, C.FP64, outputs=out64)
+    want = _oracle_counts(oracle_mod, site, real, spec, grid)
+    assert reg == int(ok.sum())
+    assert np.array_equal(got, want["counts"]), f"{(got != want['counts']).sum()} nodes differ"
+    out32 = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
+    got32, _ = _gpu_counts(site, real, spec, grid, C.FP32, outputs=out32)
+    same = (out32.naccept == out64.naccept).cpu().numpy() & (out64.status == 0).cpu().numpy()
+    drift = (out32.endpoint - out64.endpoint).abs().amax(dim=2).cpu().numpy()[same]
+    assert np.percentile(drift, 99) <= 1e-3 * spec.spacing, np.percentile(drift, 99)
+    assert np.abs(got32 - got).max() / max(reg, 1) <= 0.1
+
+
+def test_create_stochastic_capturezone_dropin(oracle_mod):
+    """The reference-signature driver: GPU draws, auto-expanding grid replay, oracle check."""
+    from onekapy_gb300.stochastic import create_stochastic_capturezone
+    spec = S.config1()
+    pf = create_stochastic_capturezone(0, 24, spec.duration, 6, spec.base, spec.c_dist, spec.p_dist,
+                                       spec.t_dist, spec.wells, spec.observations, spec.spacing,
+                                       2 * spec.spacing, True, spec.tol, spec.maxstep, seed=11)
+    real = pf.realizations
+    site = _site(spec)
+    assert pf.total_weight == 6.0
+    # the oracle replays the same expand sequence from the bounding boxes it computes itself
+    first = oracle_mod.track(site.wells.cpu().numpy()[:, :2], real.coef.cpu().numpy(),
+                             real.q.cpu().numpy(), real.aquifer.cpu().numpy(), site.release(24),
+                             (site.xt - 10, site.yt - 10, 10.0, 10.0, 3, 3), duration=spec.duration,
+                             tol=1, maxstep=10, umbra=20, confined=True, want_counts=False,
+                             xo=site.xo, yo=site.yo)
+    (xmin, ymin, nrows, ncols, _, _), frames = oracle_mod.replay_expand(
+        site.xt, site.yt, 10.0, 10.0, first["bbox"].reshape(-1, 4))
+    assert (pf.xmin, pf.ymin, pf.nrows, pf.ncols) == (xmin, ymin, nrows, ncols)
+    want = oracle_mod.track(site.wells.cpu().numpy()[:, :2], real.coef.cpu().numpy(),
+                            real.q.cpu().numpy(), real.aquifer.cpu().numpy(), site.release(24),
+                            (xmin, ymin, 10.0, 10.0, nrows, ncols), duration=spec.duration, tol=1,
+                            maxstep=10, umbra=20, confined=True, frames=frames, xo=site.xo, yo=site.yo)
+    assert np.array_equal(pf.pgrid.cpu().numpy(), want["counts"].astype(np.float64))
+
+
+def test_deterministic_capturezone_runs():
+    from onekapy_gb300.deterministic import create_deterministic_capturezone
+    spec = S.config1()
+    pf = create_deterministic_capturezone(0, 16, spec.duration, spec.base, spec.c_dist, spec.p_dist,
+                                          spec.t_dist, spec.wells, spec.observations, spec.spacing,
+                                          spec.umbra, True, spec.tol, spec.maxstep, window=spec.half)
+    assert pf.total_weight == 1.0
+    p = pf.probability()
+    assert float(p.max()) == 1.0 and float(p.min()) == 0.0

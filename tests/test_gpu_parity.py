@@ -1,0 +1,264 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference goldens and the oracle.
+
+Bars:
+  * FP64 build: visit counts bit-exact; vertices equal to the reference's
+    (bit-exact except where libm pow/log and CUDA pow/log round a step
+    factor or a logarithm differently, then within 1e-9 relative).
+  * FP32 build: endpoints within 1e-3 of the cell size of the FP64 build for
+    traces that took the same steps; capture-probability L-inf <= 0.01.
+"""
+import numpy as np
+import pytest
+import torch
+
+import known_answers as KA
+from conftest import TRACK_CASES, golden
+from gpu_helpers import golden_grid, golden_opts, golden_real, golden_site, run_golden
+
+pytestmark = pytest.mark.gpu
+
+from onekapy_gb300 import _capi as C  # noqa: E402
+from onekapy_gb300 import engine as E  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    C.load()
+    C.device()
+
+
+def _vertex_agreement(got_v, got_n, d):
+    nv = d["nvertices"]
+    assert np.array_equal(got_n, nv), "vertex counts differ from the reference"
+    mv = d["vertices"].shape[2]
+    mask = np.arange(mv)[None, None, :] < nv[:, :, None]
+    g = got_v[:, :, :mv][mask]
+    w = d["vertices"][mask]
+    same_trace = [np.array_equal(got_v[i, j, :nv[i, j]], d["vertices"][i, j, :nv[i, j]])
+                  for i in range(nv.shape[0]) for j in range(nv.shape[1])]
+    return g, w, float(np.mean(same_trace))
+
+
+@pytest.mark.parametrize("case", TRACK_CASES)
+def test_fp64_counts_bit_exact_vs_reference(case):
+    d = golden(f"track_{case}.npz")
+    r = run_golden(d, C.FP64)
+    assert r["registered"] == int(d["total_weight"])
+    assert np.array_equal(r["counts"], d["counts"]), \
+        f"{case}: {(r['counts'] != d['counts']).sum()} nodes differ"
+    g, w, frac = _vertex_agreement(r["vertices"], r["nvertices"], d)
+    assert np.allclose(g, w, rtol=1e-9, atol=1e-9)
+    assert frac >= 0.9, f"only {frac:.3f} of traces bit-identical"
+
+
+@pytest.mark.parametrize("case", ["confined_u10", "mixed_general", "unconfined_thin"])
+def test_fp32_drift_and_probability(case):
+    d = golden(f"track_{case}.npz")
+    r64 = run_golden(d, C.FP64)
+    r32 = run_golden(d, C.FP32)
+    same = r32["naccept"] == r64["naccept"]
+    assert same.mean() >= 0.9
+    drift = np.abs(r32["endpoint"] - r64["endpoint"]).max(axis=2)[same]
+    assert drift.max() <= 1e-3 * float(d["spacing"]), drift.max()
+    R = int(d["total_weight"])
+    linf = np.abs(r32["counts"] - r64["counts"]).max() / R
+    assert linf <= 0.01 + 1.0 / R  # at most one realization flips any node at this tiny R
+    mism = (r32["counts"] != r64["counts"]).sum() / max(1, (r64["counts"] > 0).sum())
+    assert mism <= 0.02, mism
+
+
+def test_fp64_expanding_grid_replay_matches_reference():
+    """compute_capturezone-style replay of the reference's growing grid."""
+    d = golden("track_expanding_u20.npz")
+    dev = C.device()
+    site, real = golden_site(d, dev), golden_real(d, dev)
+    nreal, npaths = d["nvertices"].shape
+    opts = golden_opts(d, C.FP64)
+    rel = torch.as_tensor(d["release"], device=dev)
+    first = E.TrackOutputs.alloc(nreal, npaths, dev, bbox=True, stats=False, endpoint=False)
+    E.track(site, real, rel, opts, E.Grid(0.0, 0.0, 1.0, 1.0, 1, 1), outputs=first)
+    g0 = d["grid0"]
+    (xmin, ymin, nrows, ncols, _, _), frames = E.replay_expand(
+        float(d["wells"][0, 0]), float(d["wells"][0, 1]), float(g0[2]), float(g0[3]),
+        first.bbox.reshape(-1, 4).cpu().numpy())
+    grid = E.Grid(xmin, ymin, float(g0[2]), float(g0[3]), nrows, ncols)
+    assert (xmin, ymin, nrows, ncols) == (d["grid"][0], d["grid"][1], d["grid"][4], d["grid"][5])
+    counts = torch.zeros((nrows, ncols), dtype=torch.int32, device=dev)
+    fr = torch.frombuffer(bytearray(frames.tobytes()), dtype=torch.uint8).to(dev)
+    E.track(site, real, rel, opts, grid, counts=counts, frames=fr)
+    assert np.array_equal(counts.cpu().numpy(), d["counts"])
+
+
+def test_wave_size_invariance():
+    """Counts are integer sums: any number of realization slots per wave gives the same grid."""
+    d = golden("track_confined_u10.npz")
+    a = run_golden(d, C.FP64, slots=1)
+    b = run_golden(d, C.FP64, slots=3)
+    assert np.array_equal(a["counts"], b["counts"])
+    assert np.array_equal(a["counts"], d["counts"])
+
+
+def test_attempt_cap_and_skipped_realizations():
+    d = golden("track_confined_u10.npz")
+    dev = C.device()
+    site, real = golden_site(d, dev), golden_real(d, dev)
+    real.status[1] = C.REAL_NOT_SPD
+    opts = golden_opts(d, C.FP64)
+    opts.max_attempts = 5
+    grid = golden_grid(d)
+    nreal, npaths = d["nvertices"].shape
+    out = E.TrackOutputs.alloc(nreal, npaths, dev)
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+    reg = torch.zeros(1, dtype=torch.int64, device=dev)
+    E.track(site, real, torch.as_tensor(d["release"], device=dev), opts, grid, counts=counts,
+            registered=reg, outputs=out)
+    st = out.status.cpu().numpy()
+    assert int(reg.item()) == nreal - 1
+    assert np.all(st[1] == C.TRACE_SKIPPED)
+    assert np.all(st[[0, 2]] == C.TRACE_STEP_LIMIT)
+    assert np.all(out.nattempt.cpu().numpy()[[0, 2]] == 5)
+
+
+def test_model_known_answers_gpu():
+    from onekapy_gb300.model import Model
+    m = KA.MODEL
+    mo = Model(m["base"], m["conductivity"], m["porosity"], m["thickness"], m["wells"], m["xo"],
+               m["yo"], m["coef"])
+    assert np.isclose(mo.compute_potential(*KA.POTENTIAL[0]), KA.POTENTIAL[1], rtol=KA.RTOL)
+    assert np.isclose(mo.compute_head(*KA.HEAD[0]), KA.HEAD[1], rtol=KA.RTOL)
+    assert np.allclose(mo.compute_discharge(*KA.DISCHARGE[0]), KA.DISCHARGE[1], rtol=KA.RTOL)
+    for (pt, v) in KA.VELOCITY:
+        assert np.allclose(mo.compute_velocity(*pt), v, rtol=KA.RTOL)
+
+
+def test_model_evaluate_matches_oracle(oracle_mod):
+    from onekapy_gb300.model import Model
+    d = golden("track_mixed_general.npz")
+    wells = [(w[0], w[1], w[2], q) for w, q in zip(d["wells"], d["q"][0])]
+    mo = Model(0.0, d["K"][0], d["n"][0], d["H"][0], wells, 0.0, 0.0, d["coef"][0])
+    pts = np.random.default_rng(3).uniform(-1500, 1500, size=(500, 2))
+    got = mo.evaluate(pts)
+    want = oracle_mod.evaluate(d["wells"][:, :2], d["q"][0], 0.0, d["K"][0], d["n"][0], d["H"][0],
+                               0.0, 0.0, d["coef"][0], pts)
+    for k in ("potential", "discharge", "head", "velocity"):
+        assert np.allclose(got[k], want[k], rtol=1e-13, atol=0), k
+    assert np.array_equal(got["status"], want["status"])
+
+
+def test_fit_known_answer_gpu():
+    from onekapy_gb300.model import Model
+    m = KA.MODEL
+    mo = Model(m["base"], m["conductivity"], m["porosity"], m["thickness"], m["wells"])
+    ev, cov = mo.fit_regional_flow(KA.FIT_OBS, *KA.FIT_ORIGIN)
+    assert np.allclose(ev.reshape(6), KA.FIT_EV, rtol=KA.FIT_RTOL)
+    assert np.allclose(cov, KA.FIT_COV, rtol=KA.FIT_RTOL)
+
+
+def test_fit_matches_reference_goldens():
+    from onekapy_gb300.model import Model
+    d = golden("fit_cases.npz")
+    for i in range(int(d["ncases"])):
+        w = [tuple(r) for r in d[f"wells_{i}"]]
+        mo = Model(float(d[f"base_{i}"]), float(d[f"K_{i}"]), 0.25, float(d[f"H_{i}"]), w)
+        ev, cov = mo.fit_regional_flow([tuple(r) for r in d[f"obs_{i}"]], w[0][0], w[0][1])
+        assert np.allclose(ev.reshape(6), d[f"ev_{i}"], rtol=1e-8, atol=0), i
+        assert np.allclose(cov, d[f"cov_{i}"], rtol=1e-8, atol=0), i
+
+
+def test_realize_draws_match_philox_restatement(oracle_mod):
+    """Integer Philox streams and uniform/triangular variates are bit-exact;
+    lognormal (log/cos/exp) within 1e-14 relative."""
+    dev = C.device()
+    wells = [(0.0, 0.0, 0.25, (400.0, 600.0)), (500.0, 100.0, 0.25, (100.0, 200.0, 500.0)),
+             (-300.0, 700.0, 0.25, 250.0)]
+    obs = [(x, y, 500.0 + 0.001 * x, 0.1) for x in (-900.0, -100.0, 700.0) for y in (-800.0, 50.0, 900.0)]
+    site = E.Site(wells, obs, 0.0, c_dist=E.Lognormal(np.log(10.0), 0.3), p_dist=(0.2, 0.3),
+                  t_dist=(20.0, 25.0, 30.0), device=dev)
+    seed, first, n = 123456789, 1000, 64
+    real = E.realize(site, n, seed=seed, first=first)
+    q = real.q.cpu().numpy()
+    aq = real.aquifer.cpu().numpy()
+    kinds = [(1, 400.0, 600.0, 0.0), (2, 100.0, 200.0, 500.0), (0, 250.0, 0.0, 0.0)]
+    for r in range(n):
+        for w, (k, a, b, c) in enumerate(kinds):
+            u0, u1 = oracle_mod.philox_uniforms(seed, first + r, w)
+            assert q[r, w] == oracle_mod.variate(k, a, b, c, u0, u1)
+        u0, u1 = oracle_mod.philox_uniforms(seed, first + r, 3)
+        assert np.isclose(aq[r, 0], oracle_mod.variate(3, np.log(10.0), 0.3, 0, u0, u1), rtol=1e-14)
+        u0, u1 = oracle_mod.philox_uniforms(seed, first + r, 4)
+        assert aq[r, 1] == oracle_mod.variate(1, 0.2, 0.3, 0, u0, u1)
+        u0, u1 = oracle_mod.philox_uniforms(seed, first + r, 5)
+        assert aq[r, 2] == oracle_mod.variate(2, 20.0, 25.0, 30.0, u0, u1)
+    # the fit of each drawn realization equals the NumPy restatement
+    ev = real.coef_ev.cpu().numpy()
+    cov = real.coef_cov.cpu().numpy().reshape(n, 6, 6)
+    for r in range(0, n, 7):
+        wl = [(w[0], w[1], w[2], q[r, i]) for i, w in enumerate(wells)]
+        e, c = oracle_mod.fit(obs, wl, 0.0, aq[r, 0], aq[r, 2], 0.0, 0.0)
+        assert np.allclose(ev[r], e.reshape(6), rtol=1e-8, atol=1e-12 * np.abs(e).max())
+        assert np.allclose(cov[r], c, rtol=1e-7, atol=1e-12 * np.abs(c).max())
+    # shard invariance: drawing [first+10, first+20) alone gives the same realizations
+    part = E.realize(site, 10, seed=seed, first=first + 10)
+    assert torch.equal(part.coef, real.coef[10:20])
+
+
+def test_mvn_draw_statistics():
+    """A..F draws have the fitted mean and covariance (stochastic.py:240-241)."""
+    dev = C.device()
+    wells = [(0.0, 0.0, 0.25, 500.0)]
+    rng = np.random.default_rng(5)
+    obs = [(float(x), float(y), 500.0 + 1e-3 * x - 5e-4 * y + 1e-7 * x * x, 0.1)
+           for x, y in rng.uniform(-1500, 1500, size=(25, 2))]
+    site = E.Site(wells, obs, 0.0, c_dist=10.0, p_dist=0.25, t_dist=25.0, device=dev)
+    n = 40000
+    real = E.realize(site, n, seed=7)
+    coef = real.coef.cpu().numpy()
+    ev = real.coef_ev.cpu().numpy()[0]
+    cov = real.coef_cov.cpu().numpy()[0].reshape(6, 6)
+    sd = np.sqrt(np.diag(cov))
+    z = (coef.mean(0) - ev) / (sd / np.sqrt(n))
+    assert np.all(np.abs(z) < 5), z
+    emp = np.cov(coef.T)
+    corr_emp = emp / np.outer(np.sqrt(np.diag(emp)), np.sqrt(np.diag(emp)))
+    corr = cov / np.outer(sd, sd)
+    assert np.allclose(np.sqrt(np.diag(emp)) / sd, 1, atol=0.03)
+    assert np.allclose(corr_emp, corr, atol=0.03)
+
+
+def test_rasterize_and_register_match_reference():
+    from onekapy_gb300.probabilityfield import ProbabilityField
+    d = golden("raster_cases.npz")
+    for i, (poly, g) in enumerate(zip(d["polys"], d["grids"])):
+        xmin, ymin, dx, dy, nrows, ncols, umbra, npts = g
+        pf = ProbabilityField(dx, dy, 0.0, 0.0)
+        pf.expand(-300.0, 300.0, -200.0, 250.0)
+        assert (pf.xmin, pf.ymin, pf.nrows, pf.ncols) == (xmin, ymin, int(nrows), int(ncols))
+        pts = poly[:int(npts)]
+        pf.rasterize(list(pts[:, 0]), list(pts[:, 1]), umbra)
+        want = np.unpackbits(d[f"rgrid_{i}"])[: int(nrows) * int(ncols)].reshape(int(nrows), int(ncols))
+        assert np.array_equal(pf.rgrid.cpu().numpy(), want.astype(bool)), i
+        pf.register(0.5)
+        assert np.array_equal(pf.pgrid.cpu().numpy(), 0.5 * want)
+        assert not pf.rgrid.any()
+
+
+def test_distancesquared_known_answer_gpu():
+    from onekapy_gb300.probabilityfield import ProbabilityField
+    args, want = KA.DISTANCESQUARED
+    assert np.isclose(ProbabilityField.distancesquared(*args), want, atol=1e-9)
+
+
+def test_expand_known_answer_gpu():
+    from onekapy_gb300.probabilityfield import ProbabilityField, RangeError
+    with pytest.raises(RangeError):
+        ProbabilityField(0, 0)
+    pf = ProbabilityField(1, 1)
+    with pytest.raises(RangeError):
+        pf.expand(1, 0, 1, 0)
+    pf.expand(*KA.EXPAND_REQUEST)
+    r = KA.EXPAND_RESULT
+    assert (pf.nrows, pf.ncols) == (r["nrows"], r["ncols"])
+    assert np.isclose(pf.xmin, r["xmin"]) and np.isclose(pf.xmax, r["xmax"])
+    assert np.isclose(pf.ymin, r["ymin"]) and np.isclose(pf.ymax, r["ymax"])
+    pf.expand(*KA.EXPAND_SECOND)
+    assert (pf.nrows, pf.ncols) == (r["nrows"], r["ncols"])
