@@ -129,6 +129,8 @@ typedef struct OnekaTrackOpts {
     int32_t precision;       /* ONEKA_FP64 or ONEKA_FP32 */
     int32_t max_attempts;    /* step attempts per particle before STEP_LIMIT; <= 0: 1,000,000 */
     int32_t block;           /* threads per block, multiple of 32; 0: library default */
+    int32_t window_kb;       /* shared-memory chronicle window per block in KiB (0: 32; < 0: none) */
+    int32_t pad;
 } OnekaTrackOpts;
 
 /* Optional per-particle outputs ([nreal][npaths] leading); any pointer may be NULL. */

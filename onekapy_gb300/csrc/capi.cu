@@ -1,4 +1,5 @@
 // capi.cu -- extern "C" entry points of liboneka_gb300.so (include/oneka_gb300.h).
+#include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -54,6 +55,37 @@ using namespace oneka;
 
 static bool grid_ok(const OnekaGrid* g) {
     return g && g->nrows > 0 && g->ncols > 0 && g->dx > 0 && g->dy > 0;
+}
+
+// The shared-memory chronicle window: the whole grid when it fits the
+// budget, else a window about square in nodes centred on the regional origin
+// (the target well), where traces start and overlap most.
+static void set_window(TrackLaunch& L, const OnekaGrid& g, int window_kb) {
+    L.win_r0 = L.win_w0 = L.win_rows = L.win_words = 0;
+    if (window_kb < 0) return;
+    const long long budget = (long long)(window_kb == 0 ? 32 : window_kb) * 256;   // words
+    const int wpr = words_per_row(g.ncols);
+    if ((long long)g.nrows * wpr <= budget) {
+        L.win_rows = g.nrows;
+        L.win_words = wpr;
+        return;
+    }
+    int ww = 1;
+    while ((long long)(ww + 1) * (ww + 1) * 32 <= budget) ++ww;
+    if (ww > wpr) ww = wpr;
+    long long wr = budget / ww;
+    if (wr > g.nrows) wr = g.nrows;
+    const int row_t = (int)floor((L.yt - g.ymin) / g.dy + 0.5);
+    const int col_t = (int)floor((L.xt - g.xmin) / g.dx + 0.5);
+    int r0 = row_t - (int)(wr / 2), w0 = (col_t >> 5) - ww / 2;
+    if (r0 > g.nrows - (int)wr) r0 = g.nrows - (int)wr;
+    if (r0 < 0) r0 = 0;
+    if (w0 > wpr - ww) w0 = wpr - ww;
+    if (w0 < 0) w0 = 0;
+    L.win_r0 = r0;
+    L.win_w0 = w0;
+    L.win_rows = (int)wr;
+    L.win_words = ww;
 }
 
 extern "C" {
@@ -142,6 +174,7 @@ int oneka_track(const OnekaSite* site, const OnekaRealizations* real, int32_t nr
     L.registered = (unsigned long long*)registered;
     if (out) L.out = *out;
     L.max_attempts = opts->max_attempts > 0 ? opts->max_attempts : kDefaultMaxAttempts;
+    set_window(L, *grid, opts->window_kb);
 
     int wave = nreal < 65535 ? nreal : 65535;
     if (!counts && scratch) {

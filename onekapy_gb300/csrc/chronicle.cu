@@ -71,8 +71,13 @@ __global__ void rasterize_kernel(OnekaGrid g, OnekaFrame f, const double* __rest
     if (i + 1 >= n) return;
     long long ntest = 0, natom = 0;
     int rlo = 0x7fffffff, rhi = -1;
-    insert64(mask, wpr, g.nrows, g.ncols, f, g.dx, g.dy, umbra, xy[2 * i], xy[2 * i + 1],
-             xy[2 * i + 2], xy[2 * i + 3], ntest, natom, rlo, rhi);
+    Chron ch;
+    ch.slot = mask;
+    ch.win = nullptr;
+    ch.wpr = wpr;
+    ch.r0 = ch.w0 = ch.nr = ch.nw = 0;
+    insert64(ch, g.nrows, g.ncols, f, g.dx, g.dy, umbra, xy[2 * i], xy[2 * i + 1], xy[2 * i + 2],
+             xy[2 * i + 3], ntest, natom, rlo, rhi);
 }
 
 __global__ void distancesquared_kernel(const double* __restrict__ abc, double* __restrict__ d2, long long n) {

@@ -35,7 +35,52 @@ struct TrackLaunch {
     unsigned long long* registered;
     OnekaTrackOut out;
     int max_attempts;
+    // shared-memory window of each realization slot: rows [win_r0, win_r0 + win_rows),
+    // words [win_w0, win_w0 + win_words) of every row; win_rows == 0: no window
+    int win_r0, win_w0, win_rows, win_words;
 };
+
+// Where a chronicle mark goes: the block's shared-memory window of the slot
+// when the word lies inside it, else the slot in global memory.
+struct Chron {
+    uint32_t* slot;
+    uint32_t* win;
+    int wpr, r0, w0, nr, nw;
+    __device__ __forceinline__ void orw(int gi, int w, uint32_t bits) const {
+        const int ri = gi - r0, wi = w - w0;
+        if (win && (unsigned)ri < (unsigned)nr && (unsigned)wi < (unsigned)nw)
+            atomicOr(win + ri * nw + wi, bits);
+        else
+            atomicOr(slot + (long long)gi * wpr + w, bits);
+    }
+};
+
+__device__ __forceinline__ Chron make_chron(const TrackLaunch& L, uint32_t* slot, uint32_t* win) {
+    Chron c;
+    c.slot = slot;
+    c.win = (slot && L.win_rows > 0) ? win : nullptr;
+    c.wpr = L.wpr;
+    c.r0 = L.win_r0;
+    c.w0 = L.win_w0;
+    c.nr = L.win_rows;
+    c.nw = L.win_words;
+    return c;
+}
+
+// Zero the block's window (before the first mark) ...
+__device__ __forceinline__ void window_clear(const Chron& c) {
+    if (!c.win) return;
+    for (int i = threadIdx.x; i < c.nr * c.nw; i += blockDim.x) c.win[i] = 0u;
+}
+
+// ... and OR its nonzero words into the global slot (after the last mark).
+__device__ __forceinline__ void window_flush(const Chron& c) {
+    if (!c.win) return;
+    for (int i = threadIdx.x; i < c.nr * c.nw; i += blockDim.x) {
+        const uint32_t v = c.win[i];
+        if (v) atomicOr(c.slot + (long long)(c.r0 + i / c.nw) * c.wpr + (c.w0 + i % c.nw), v);
+    }
+}
 
 // A realization slot: the bitmask (nrows rows of words_per_row words), padded
 // to a multiple of 4 words, then a 4-word header { h0, h1, 0, 0 } recording
@@ -128,7 +173,7 @@ __device__ __forceinline__ bool in_umbra64(double bax, double bay, double cax, d
 // ProbabilityField.insert (probabilityfield.py:296-310) into a realization
 // bitmask: every node of the frame within umbra of segment a-b is OR-ed in,
 // one atomicOr per touched 32-node word of a row.
-__device__ __forceinline__ void insert64(uint32_t* __restrict__ slot, int wpr, int gnrows, int gncols,
+__device__ __forceinline__ void insert64(const Chron& ch, int gnrows, int gncols,
                                          const OnekaFrame& f, double dx, double dy, double umbra,
                                          double ax, double ay, double bx, double by,
                                          long long& ntest, long long& natom, int& rlo, int& rhi) {
@@ -153,7 +198,6 @@ __device__ __forceinline__ void insert64(uint32_t* __restrict__ slot, int wpr, i
         const double cay = cy - ay;
         uint32_t acc = 0;
         int curw = -1;
-        uint32_t* row = slot + (long long)gi * wpr;
         for (int j = left; j < right; ++j) {
             const int gj = j + f.coff;
             if (gj < 0 || gj >= gncols) continue;
@@ -162,7 +206,7 @@ __device__ __forceinline__ void insert64(uint32_t* __restrict__ slot, int wpr, i
             if (in_umbra64(bax, bay, cax, cay, length2, inv, fast_ok, u2)) {
                 const int w = gj >> 5;
                 if (w != curw) {
-                    if (acc) { atomicOr(row + curw, acc); ++natom; }
+                    if (acc) { ch.orw(gi, curw, acc); ++natom; }
                     curw = w;
                     acc = 0;
                 }
@@ -170,7 +214,7 @@ __device__ __forceinline__ void insert64(uint32_t* __restrict__ slot, int wpr, i
             }
         }
         if (curw >= 0) {
-            if (acc) { atomicOr(row + curw, acc); ++natom; }
+            if (acc) { ch.orw(gi, curw, acc); ++natom; }
             rlo = gi < rlo ? gi : rlo;
             rhi = gi > rhi ? gi : rhi;
         }

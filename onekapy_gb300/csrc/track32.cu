@@ -95,17 +95,33 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-// Chronicle one segment in FP32 (node test: distance to the segment < umbra).
-__device__ __forceinline__ void insert32(uint32_t* __restrict__ slot, int wpr, int gnrows, int gncols,
-                                         const OnekaFrame& f, float fx0, float fy0, float dx, float dy,
-                                         float umbra, float ax, float ay, float bx, float by,
-                                         long long& ntest, long long& natom, int& rlo, int& rhi) {
+// OR the nodes gj in [glo, ghi] of grid row gi into the chronicle.
+__device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int ghi, long long& natom) {
+    int w = glo >> 5;
+    const int wl = ghi >> 5;
+    uint32_t m = 0xffffffffu << (glo & 31);
+    for (; w <= wl; ++w) {
+        if (w == wl) m &= 0xffffffffu >> (31 - (ghi & 31));
+        ch.orw(gi, w, m);
+        ++natom;
+        m = 0xffffffffu;
+    }
+}
+
+// Chronicle one segment in FP32: for every grid row the nodes within umbra
+// of the segment form one interval, the row's intersection with the capsule
+// (the two end disks and the band between them); the interval's nodes are
+// set as whole bit ranges.  Nodes strictly closer than umbra are marked, as
+// in ProbabilityField.insert (probabilityfield.py:296-310); FP32 rounding can
+// move a node lying within ~1e-6 m of the boundary across it.
+__device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols, const OnekaFrame& f,
+                                         float fx0, float fy0, float dx, float dy, float umbra,
+                                         float ax, float ay, float bx, float by, long long& ntest,
+                                         long long& natom, int& rlo, int& rhi) {
     const float bax = bx - ax;
     const float bay = by - ay;
     const float length2 = bax * bax + bay * bay;
     if (!(length2 > 0.0f)) return;           // the reference's 0/0 marks nothing
-    const float inv = 1.0f / length2;
-    const float u2 = umbra * umbra;
     int left, right, bottom, top;
     if (!clip_range(floorf((fminf(ax, bx) - umbra - fx0) / dx),
                     floorf((fmaxf(ax, bx) + umbra - fx0) / dx) + 1.0f, f.ncols, left, right))
@@ -114,58 +130,92 @@ __device__ __forceinline__ void insert32(uint32_t* __restrict__ slot, int wpr, i
                     floorf((fmaxf(ay, by) + umbra - fy0) / dy) + 1.0f, f.nrows, bottom, top))
         return;
     ntest += (long long)(right - left) * (top - bottom);
+    const float u2 = umbra * umbra;
+    const float uL = umbra * sqrtf(length2);
+    const float inv_bay = (bay != 0.0f) ? 1.0f / bay : 0.0f;
+    const float inv_bax = (bax != 0.0f) ? 1.0f / bax : 0.0f;
+    const float inv_dx = 1.0f / dx;
     for (int i = bottom; i < top; ++i) {
         const int gi = i + f.roff;
         if (gi < 0 || gi >= gnrows) continue;
-        const float cay = (fy0 + (float)i * dy) - ay;
-        uint32_t acc = 0;
-        int curw = -1;
-        uint32_t* row = slot + (long long)gi * wpr;
-        for (int j = left; j < right; ++j) {
-            const int gj = j + f.coff;
-            if (gj < 0 || gj >= gncols) continue;
-            const float cax = (fx0 + (float)j * dx) - ax;
-            const float tt = fminf(fmaxf((bax * cax + bay * cay) * inv, 0.0f), 1.0f);
-            const float ex = cax - tt * bax;
-            const float ey = cay - tt * bay;
-            if (ex * ex + ey * ey < u2) {
-                const int w = gj >> 5;
-                if (w != curw) {
-                    if (acc) { atomicOr(row + curw, acc); ++natom; }
-                    curw = w;
-                    acc = 0;
-                }
-                acc |= 1u << (gj & 31);
-            }
+        const float cy = fy0 + (float)i * dy;
+        const float cay = cy - ay, cby = cy - by;
+        float lo = INFINITY, hi = -INFINITY;
+        const float ha = u2 - cay * cay;
+        if (ha > 0.0f) { const float h = sqrtf(ha); lo = ax - h; hi = ax + h; }
+        const float hb = u2 - cby * cby;
+        if (hb > 0.0f) { const float h = sqrtf(hb); lo = fminf(lo, bx - h); hi = fmaxf(hi, bx + h); }
+        // band: s = x - ax with |bay s - bax cay| < u L and 0 <= bax s + bay cay <= L^2
+        float slo = -INFINITY, shi = INFINITY;
+        const float bc = bax * cay;
+        if (bay != 0.0f) {
+            const float c1 = (bc - uL) * inv_bay, c2 = (bc + uL) * inv_bay;
+            slo = fminf(c1, c2);
+            shi = fmaxf(c1, c2);
+        } else if (!(fabsf(bc) < uL)) {
+            slo = INFINITY;
         }
-        if (curw >= 0) {
-            if (acc) { atomicOr(row + curw, acc); ++natom; }
-            rlo = gi < rlo ? gi : rlo;
-            rhi = gi > rhi ? gi : rhi;
+        const float yc = bay * cay;
+        if (bax != 0.0f) {
+            const float d1 = -yc * inv_bax, d2 = (length2 - yc) * inv_bax;
+            slo = fmaxf(slo, fminf(d1, d2));
+            shi = fminf(shi, fmaxf(d1, d2));
+        } else if (!(yc >= 0.0f && yc <= length2)) {
+            slo = INFINITY;
         }
+        if (slo < shi) { lo = fminf(lo, ax + slo); hi = fmaxf(hi, ax + shi); }
+        if (!(lo < hi)) continue;
+        int jlo = (int)fmaxf(ceilf((lo - fx0) * inv_dx), (float)left);
+        int jhi = (int)fminf(floorf((hi - fx0) * inv_dx), (float)(right - 1));
+        // strictly inside: drop an end node that sits on the boundary
+        if (jlo <= jhi && fx0 + (float)jlo * dx <= lo) ++jlo;
+        if (jlo <= jhi && fx0 + (float)jhi * dx >= hi) --jhi;
+        int glo = jlo + f.coff, ghi = jhi + f.coff;
+        glo = glo < 0 ? 0 : glo;
+        ghi = ghi >= gncols ? gncols - 1 : ghi;
+        if (glo > ghi) continue;
+        or_span(ch, gi, glo, ghi, natom);
+        rlo = gi < rlo ? gi : rlo;
+        rhi = gi > rhi ? gi : rhi;
     }
 }
+
+template <bool CONFINED>
+__device__ __forceinline__ void trace32(const TrackLaunch& L, int r, int p, long long idx, const float4* sm32,
+                                        const Chron& ch);
 
 template <bool CONFINED>
 __global__ void __launch_bounds__(256) track32_kernel(const TrackLaunch L) {
     extern __shared__ float4 sm32[];
     const int k = blockIdx.y;
     const int r = L.r0 + k;
+    uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
+    const Chron ch = make_chron(L, slot, reinterpret_cast<uint32_t*>(sm32 + L.nwells));
     for (int i = threadIdx.x; i < L.nwells; i += blockDim.x) {
         const double q = L.q[(long long)r * L.nwells + i];
         sm32[i] = make_float4((float)(L.wells[3 * i] - L.xt), (float)(L.wells[3 * i + 1] - L.yt),
                               (float)(-q * 0.15915494309189535), (float)(q * 0.07957747154594767));
     }
+    window_clear(ch);
     __syncthreads();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const long long idx = (long long)r * L.npaths + p;
     const bool skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
     if (!skip && blockIdx.x == 0 && threadIdx.x == 0 && L.registered) atomicAdd(L.registered, 1ull);
-    if (p >= L.npaths) return;
-    if (skip) {
-        if (L.out.status) L.out.status[idx] = kTraceSkipped;
-        return;
+    if (p < L.npaths) {
+        if (skip) {
+            if (L.out.status) L.out.status[idx] = kTraceSkipped;
+        } else {
+            trace32<CONFINED>(L, r, p, idx, sm32, ch);
+        }
     }
+    __syncthreads();
+    window_flush(ch);
+}
+
+template <bool CONFINED>
+__device__ __forceinline__ void trace32(const TrackLaunch& L, int r, int p, long long idx, const float4* sm32,
+                                        const Chron& ch) {
 
     Model32 m;
     m.w = sm32;
@@ -185,7 +235,7 @@ __global__ void __launch_bounds__(256) track32_kernel(const TrackLaunch L) {
     const OnekaFrame f = frame_of(L, r, p);
     const float fx0 = (float)(f.xmin - L.xt);
     const float fy0 = (float)(f.ymin - L.yt);
-    uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
+    uint32_t* slot = ch.slot;
     const float gdx = (float)L.grid.dx, gdy = (float)L.grid.dy, umbra = (float)L.opts.umbra;
 
     const double dur = L.opts.duration;
@@ -281,7 +331,7 @@ __global__ void __launch_bounds__(256) track32_kernel(const TrackLaunch L) {
                 yl = e;
                 const float bxn = xh + xl, byn = yh + yl;
                 if (slot)
-                    insert32(slot, L.wpr, L.grid.nrows, L.grid.ncols, f, fx0, fy0, gdx, gdy, umbra,
+                    insert32(ch, L.grid.nrows, L.grid.ncols, f, fx0, fy0, gdx, gdy, umbra,
                              ax, ay, bxn, byn, ntest, natom, rlo, rhi);
                 bx0 = fminf(bx0, bxn); bx1 = fmaxf(bx1, bxn);
                 by0 = fminf(by0, byn); by1 = fmaxf(by1, byn);
@@ -321,11 +371,14 @@ cudaError_t launch_track32(const TrackLaunch& L, cudaStream_t s) {
     const int block = L.opts.block > 0 ? L.opts.block : 128;
     dim3 grid((unsigned)((L.npaths + block - 1) / block), (unsigned)L.nr);
     if (grid.x == 0) grid.x = 1;
-    const size_t smem = sizeof(float4) * (size_t)L.nwells;
-    if (L.opts.confined)
+    const size_t smem = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)L.win_rows * L.win_words;
+    if (L.opts.confined) {
+        cudaFuncSetAttribute(track32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         track32_kernel<true><<<grid, block, smem, s>>>(L);
-    else
+    } else {
+        cudaFuncSetAttribute(track32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         track32_kernel<false><<<grid, block, smem, s>>>(L);
+    }
     return cudaGetLastError();
 }
 

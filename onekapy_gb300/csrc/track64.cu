@@ -12,6 +12,7 @@
 //   oneka/probabilityfield.py:264-339  rasterize / insert (per accepted segment)
 #include <math.h>
 
+#include "crpow.cuh"
 #include "oneka_internal.cuh"
 
 namespace oneka {
@@ -89,6 +90,10 @@ struct VertexSink {
 };
 
 template <bool CONFINED>
+__device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, const double* wx,
+                                        const double* wy, const double* wq, const Chron& ch);
+
+template <bool CONFINED>
 __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
     extern __shared__ double sm64[];
     const int k = blockIdx.y;
@@ -96,21 +101,33 @@ __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
     double* wx = sm64;
     double* wy = sm64 + L.nwells;
     double* wq = sm64 + 2 * L.nwells;
+    uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
+    const Chron ch = make_chron(L, slot, reinterpret_cast<uint32_t*>(sm64 + 3 * L.nwells));
     for (int i = threadIdx.x; i < L.nwells; i += blockDim.x) {
         wx[i] = L.wells[3 * i];
         wy[i] = L.wells[3 * i + 1];
         wq[i] = L.q[(long long)r * L.nwells + i];
     }
+    window_clear(ch);
     __syncthreads();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const long long idx = (long long)r * L.npaths + p;
     const bool skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
     if (!skip && blockIdx.x == 0 && threadIdx.x == 0 && L.registered) atomicAdd(L.registered, 1ull);
-    if (p >= L.npaths) return;
-    if (skip) {
-        if (L.out.status) L.out.status[idx] = kTraceSkipped;
-        return;
+    if (p < L.npaths) {
+        if (skip) {
+            if (L.out.status) L.out.status[idx] = kTraceSkipped;
+        } else {
+            trace64<CONFINED>(L, r, p, idx, wx, wy, wq, ch);
+        }
     }
+    __syncthreads();
+    window_flush(ch);
+}
+
+template <bool CONFINED>
+__device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, const double* wx,
+                                        const double* wy, const double* wq, const Chron& ch) {
 
     Model64 m;
     m.wx = wx;
@@ -126,7 +143,7 @@ __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
     m.H = L.aquifer[3LL * r + 2];
 
     const OnekaFrame f = frame_of(L, r, p);
-    uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
+    uint32_t* slot = ch.slot;
 
     const double dur = L.opts.duration;
     const double tol = L.opts.tol;
@@ -189,7 +206,7 @@ __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
             if ((est < tol) && (ds < maxstep)) {
                 t = t + dt;
                 if (slot)
-                    insert64(slot, L.wpr, L.grid.nrows, L.grid.ncols, f, L.grid.dx, L.grid.dy,
+                    insert64(ch, L.grid.nrows, L.grid.ncols, f, L.grid.dx, L.grid.dy,
                              L.opts.umbra, x, y, xn, yn, ntest, natom, rlo, rhi);
                 k1x = k7x;
                 k1y = k7y;
@@ -198,10 +215,19 @@ __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
                 vs.push(x, y);
                 ++acc;
             }
-            double fac = pow(tol / (est + DP::eps), 1.0 / 5.0);
+            // dt = 0.9 * min((tol/(est+EPS))**(1/5), maxstep/(ds+EPS), 10) * dt  (:247)
             const double fstep = maxstep / (ds + DP::eps);
-            if (fstep < fac) fac = fstep;
-            if (10.0 < fac) fac = 10.0;
+            const double xq = tol / (est + DP::eps);
+            double lower = fstep;
+            if (10.0 < lower) lower = 10.0;
+            double fac;
+            if (pow(xq, 0.2) > lower * (1.0 + 1e-13)) {
+                fac = lower;                        // the power cannot be the minimum
+            } else {
+                fac = cr_pow_fifth(xq);             // it may be: evaluate it exactly
+                if (fstep < fac) fac = fstep;
+                if (10.0 < fac) fac = 10.0;
+            }
             dt = 0.9 * fac * dt;
         }
     }
@@ -229,11 +255,14 @@ cudaError_t launch_track64(const TrackLaunch& L, cudaStream_t s) {
     const int block = 128;
     dim3 grid((unsigned)((L.npaths + block - 1) / block), (unsigned)L.nr);
     if (grid.x == 0) grid.x = 1;
-    const size_t smem = sizeof(double) * 3 * (size_t)L.nwells;
-    if (L.opts.confined)
+    const size_t smem = sizeof(double) * 3 * (size_t)L.nwells + 4 * (size_t)L.win_rows * L.win_words;
+    if (L.opts.confined) {
+        cudaFuncSetAttribute(track64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         track64_kernel<true><<<grid, block, smem, s>>>(L);
-    else
+    } else {
+        cudaFuncSetAttribute(track64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         track64_kernel<false><<<grid, block, smem, s>>>(L);
+    }
     return cudaGetLastError();
 }
 
