@@ -210,6 +210,35 @@ ONEKA_API int oneka_track(const OnekaSite* site, const OnekaRealizations* real, 
                 int64_t* registered, const OnekaTrackOut* out, void* scratch,
                 size_t scratch_bytes, void* stream);
 
+/* Size of the fixed scratch array inside the library that oneka_track_noalloc uses. */
+#define ONEKA_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/*
+ * oneka_track for callers that cannot allocate device memory.  No counterpart
+ * in the reference: it exists for hosts that cannot call cudaMalloc -- a
+ * plugin whose device memory the host's own allocator has already divided
+ * up, or a binding that can only pass buffers the host owns.  It takes the
+ * same arguments as oneka_track minus the scratch, which comes from a
+ * file-scope array of ONEKA_NOALLOC_SCRATCH_BYTES (32 MiB) inside the library,
+ * held by every GPU that loads the library until the process exits.
+ *   - Inputs and outputs are still the caller's device buffers.
+ *   - A grid whose realization slot (oneka_track_scratch_bytes(grid, 1))
+ *     exceeds 32 MiB is rejected with ONEKA_ERR_SCRATCH; smaller grids run
+ *     32 MiB / slot realizations per launch.
+ *   - The call allocates nothing: no cudaMalloc/cudaFree, no allocating
+ *     library routine.
+ *   - Every call on a device shares the array and clears the part it uses
+ *     first; calls that overlap on the GPU (other streams or threads) race on
+ *     it, so order them on one stream.
+ *   - The first call on each device (with that device current) looks up the
+ *     array's device address and caches it; make that first call before any
+ *     stream capture.
+ */
+ONEKA_API int oneka_track_noalloc(const OnekaSite* site, const OnekaRealizations* real, int32_t nreal,
+                                  const double* release, int32_t npaths, const OnekaTrackOpts* opts,
+                                  const OnekaGrid* grid, const OnekaFrame* frames, int32_t* counts,
+                                  int64_t* registered, const OnekaTrackOut* out, void* stream);
+
 /*
  * Model evaluation at npts points (model.py:207-427): potential, discharge
  * [npts][2], head, velocity [npts][2] (general when confined == 0, else the

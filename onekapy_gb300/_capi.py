@@ -24,7 +24,9 @@ FP64, FP32 = 0, 1
 
 EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_realize",
            "oneka_track_scratch_bytes", "oneka_track", "oneka_evaluate", "oneka_rasterize",
-           "oneka_register_weighted", "oneka_distancesquared", "oneka_fma_peak"]
+           "oneka_register_weighted", "oneka_distancesquared", "oneka_fma_peak",
+           "oneka_track_noalloc"]
+NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
 _D = ctypes.c_double
@@ -101,6 +103,11 @@ def load() -> ctypes.CDLL:
         L.oneka_track.argtypes = [ctypes.POINTER(OnekaSite), ctypes.POINTER(OnekaRealizations), _I,
                                   _P, _I, ctypes.POINTER(OnekaTrackOpts), ctypes.POINTER(OnekaGrid),
                                   _P, _P, _P, ctypes.POINTER(OnekaTrackOut), _P, ctypes.c_size_t, _P]
+        L.oneka_track_noalloc.restype = ctypes.c_int
+        L.oneka_track_noalloc.argtypes = [ctypes.POINTER(OnekaSite), ctypes.POINTER(OnekaRealizations), _I,
+                                          _P, _I, ctypes.POINTER(OnekaTrackOpts),
+                                          ctypes.POINTER(OnekaGrid), _P, _P, _P,
+                                          ctypes.POINTER(OnekaTrackOut), _P]
         L.oneka_evaluate.restype = ctypes.c_int
         L.oneka_evaluate.argtypes = [ctypes.POINTER(OnekaSite), _P, _D, _D, _D,
                                      ctypes.POINTER(ctypes.c_double), _P, ctypes.c_int64, _I, _P, _P,

@@ -34,6 +34,7 @@ UNITS = {
     "track64.cu": ["--fmad=false"],
     "track32.cu": ["--fmad=true", "--use_fast_math"],
     "probe.cu": ["--fmad=true"],
+    "noalloc.cu": ["--fmad=false"],
 }
 
 
