@@ -128,9 +128,10 @@ typedef struct OnekaTrackOpts {
     int32_t confined;        /* 1: compute_velocity_confined; 0: compute_velocity */
     int32_t precision;       /* ONEKA_FP64 or ONEKA_FP32 */
     int32_t max_attempts;    /* step attempts per particle before STEP_LIMIT; <= 0: 1,000,000 */
-    int32_t block;           /* threads per block, multiple of 32; 0: library default */
+    int32_t block;           /* threads per block: 32, 64, 128 or 256; 0: 128 */
     int32_t window_kb;       /* shared-memory chronicle window per block in KiB (0: 32; < 0: none) */
-    int32_t pad;
+    int32_t occupancy;       /* FP32 build: resident blocks per SM to compile for (4, 6, 8 at 128
+                                threads; 2, 3 at 256); 0: 4 */
 } OnekaTrackOpts;
 
 /* Optional per-particle outputs ([nreal][npaths] leading); any pointer may be NULL. */

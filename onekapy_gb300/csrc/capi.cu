@@ -143,7 +143,8 @@ int oneka_track(const OnekaSite* site, const OnekaRealizations* real, int32_t nr
     ONEKA_CHECK_ARG(real->coef && real->q && real->aquifer, "realization arrays");
     ONEKA_CHECK_ARG(opts->precision == ONEKA_FP64 || opts->precision == ONEKA_FP32, "precision");
     ONEKA_CHECK_ARG(opts->tol > 0 && opts->maxstep > 0 && opts->umbra >= 0, "tol/maxstep/umbra");
-    ONEKA_CHECK_ARG(opts->block == 0 || (opts->block % 32 == 0 && opts->block <= 256), "block");
+    ONEKA_CHECK_ARG(opts->block == 0 || opts->block == 32 || opts->block == 64 || opts->block == 128 ||
+                    opts->block == 256, "block must be 32, 64, 128 or 256");
     ONEKA_CHECK_ARG(!out || out->max_vertices >= 0, "max_vertices");
     ONEKA_CHECK_ARG(!out || !out->vertices || out->max_vertices > 0, "vertices without max_vertices");
     if (nreal == 0) return ONEKA_OK;

@@ -1,4 +1,4 @@
-// track32.cu -- FP32 fast tracker: one thread per particle.
+// track32.cu -- FP32 fast tracker: persistent lanes over a realization's particles.
 //
 // Same algorithm as the FP64 parity build (oneka/capturezone.py:198-253 step
 // control, oneka/model.py:269-427 velocity, oneka/probabilityfield.py:264-339
@@ -7,9 +7,17 @@
 //     a float pair (hi + lo) updated with an error-free two-sum, so the
 //     position keeps ~48 bits over hundreds of steps;
 //   * well terms are summed with Kahan compensation (discharge and potential);
-//   * where the potential lies within 1% of K*H^2/2 (the confined/unconfined
-//     switch) the head is inverted in FP64 from the compensated potential;
+//   * the head is inverted from the compensated potential in FP32 (the
+//     inversion is well conditioned; see feval32);
 //   * elapsed time is kept in FP64.
+//
+// Work layout: one block per realization (or per chunk of its particles when
+// the realizations alone cannot fill the GPU).  Each lane takes the next
+// particle from a shared counter as soon as its trace ends, so a block's
+// lanes stay busy until its last particles, and no lane waits for the
+// slowest trace of a fixed group.  The Dormand-Prince stage vectors live in
+// shared memory ([stage][x|y][lane]), so the velocity evaluation is inlined
+// once and the per-thread state stays small.
 #include <math.h>
 
 #include "oneka_internal.cuh"
@@ -24,7 +32,9 @@ struct Model32 {
     float c0, c1, c2, c3, c4, c5;
     float K, n, H;
     float inv_hn;        // 1 / (H n)
-    double kh2;          // 0.5 K H^2 in FP64
+    float kh2f;          // 0.5 K H^2
+    float inv_k;         // 1 / K
+    float inv_kh;        // 1 / (K H)
 };
 
 struct Kahan {
@@ -62,25 +72,20 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
         ky = -(qy.s * m.inv_hn);
         return true;
     }
+    // Head from the compensated potential (model.py:341-350).  The inversion
+    // itself is well conditioned (sqrt halves relative errors; the confined
+    // branch is linear), so FP32 keeps the digits the compensated sum
+    // delivers.  An FP64 inversion near the aquifer top would add nothing to
+    // an FP32 result and, on GB300, costs the whole warp ~1000 FP64-pipe
+    // cycles whenever one lane takes it.
     const float phi = pot.s - pot.c;
     if (phi <= 0.0f) return false;
+    const float kh2 = m.kh2f;
     float head;
-    const float kh2 = (float)m.kh2;
-    if (fabsf(phi - kh2) < 0.01f * kh2) {
-        // Near the top of the aquifer: invert in FP64 from the compensated sum.
-        const double pd = (double)pot.s - (double)pot.c;
-        if (pd <= 0.0) return false;
-        double hd;
-        if (pd < m.kh2)
-            hd = sqrt(2.0 * pd / (double)m.K);
-        else
-            hd = (pd + m.kh2) / ((double)m.K * (double)m.H);
-        head = (float)hd;
-    } else if (phi < kh2) {
-        head = sqrtf(2.0f * phi / m.K);
-    } else {
-        head = (phi + kh2) / (m.K * m.H);
-    }
+    if (phi < kh2)
+        head = sqrtf(2.0f * phi * m.inv_k);
+    else
+        head = (phi + kh2) * m.inv_kh;
     if (head <= 0.0f) return false;
     const float inv = (head > m.H) ? m.inv_hn : 1.0f / (head * m.n);
     kx = -(qx.s * inv);
@@ -93,6 +98,31 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
+}
+
+// Conversions without the FP64 pipe.  On GB300, I2F/F2I and float rounding
+// instructions issue on the (narrow) FP64 pipe; these use an FADD with
+// 1.5 * 2^23, whose low mantissa bits then hold the integer, and integer
+// arithmetic.  Exact for |values| < 2^22 (arguments are clamped to that).
+constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+
+__device__ __forceinline__ float i2f_small(int i) { return __fsub_rn(__int_as_float(kMagicBits + i), kMagic); }
+
+__device__ __forceinline__ int floor_small(float x) {
+    x = fminf(fmaxf(x, -4.0e6f), 4.0e6f);
+    const float b = __fadd_rn(x, kMagic);               // round to nearest integer (+M)
+    const float r = __fsub_rn(b, kMagic);
+    return (__float_as_int(b) - kMagicBits) - (r > x ? 1 : 0);
+}
+
+__device__ __forceinline__ int ceil_small(float x) { return -floor_small(-x); }
+
+// clip_range for integer bounds [lo, hi) of a range of n nodes.
+__device__ __forceinline__ bool clip_int(int lo, int hi, int n, int& ilo, int& ihi) {
+    ilo = lo < 0 ? 0 : lo;
+    ihi = hi > n ? n : hi;
+    return ilo < ihi;
 }
 
 // OR the nodes gj in [glo, ghi] of grid row gi into the chronicle.
@@ -114,31 +144,32 @@ __device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int gh
 // set as whole bit ranges.  Nodes strictly closer than umbra are marked, as
 // in ProbabilityField.insert (probabilityfield.py:296-310); FP32 rounding can
 // move a node lying within ~1e-6 m of the boundary across it.
-__device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols, const OnekaFrame& f,
-                                         float fx0, float fy0, float dx, float dy, float umbra,
+__device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols, int coff, int roff,
+                                         int fncols, int fnrows, float fx0, float fy0, float dx, float dy,
+                                         float umbra,
                                          float ax, float ay, float bx, float by, long long& ntest,
                                          long long& natom, int& rlo, int& rhi) {
     const float bax = bx - ax;
     const float bay = by - ay;
     const float length2 = bax * bax + bay * bay;
     if (!(length2 > 0.0f)) return;           // the reference's 0/0 marks nothing
+    const float inv_dx = 1.0f / dx, inv_dy = 1.0f / dy;
     int left, right, bottom, top;
-    if (!clip_range(floorf((fminf(ax, bx) - umbra - fx0) / dx),
-                    floorf((fmaxf(ax, bx) + umbra - fx0) / dx) + 1.0f, f.ncols, left, right))
+    if (!clip_int(floor_small((fminf(ax, bx) - umbra - fx0) * inv_dx),
+                  floor_small((fmaxf(ax, bx) + umbra - fx0) * inv_dx) + 1, fncols, left, right))
         return;
-    if (!clip_range(floorf((fminf(ay, by) - umbra - fy0) / dy),
-                    floorf((fmaxf(ay, by) + umbra - fy0) / dy) + 1.0f, f.nrows, bottom, top))
+    if (!clip_int(floor_small((fminf(ay, by) - umbra - fy0) * inv_dy),
+                  floor_small((fmaxf(ay, by) + umbra - fy0) * inv_dy) + 1, fnrows, bottom, top))
         return;
     ntest += (long long)(right - left) * (top - bottom);
     const float u2 = umbra * umbra;
     const float uL = umbra * sqrtf(length2);
     const float inv_bay = (bay != 0.0f) ? 1.0f / bay : 0.0f;
     const float inv_bax = (bax != 0.0f) ? 1.0f / bax : 0.0f;
-    const float inv_dx = 1.0f / dx;
     for (int i = bottom; i < top; ++i) {
-        const int gi = i + f.roff;
+        const int gi = i + roff;
         if (gi < 0 || gi >= gnrows) continue;
-        const float cy = fy0 + (float)i * dy;
+        const float cy = fy0 + i2f_small(i) * dy;
         const float cay = cy - ay, cby = cy - by;
         float lo = INFINITY, hi = -INFINITY;
         const float ha = u2 - cay * cay;
@@ -165,12 +196,12 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
         }
         if (slo < shi) { lo = fminf(lo, ax + slo); hi = fmaxf(hi, ax + shi); }
         if (!(lo < hi)) continue;
-        int jlo = (int)fmaxf(ceilf((lo - fx0) * inv_dx), (float)left);
-        int jhi = (int)fminf(floorf((hi - fx0) * inv_dx), (float)(right - 1));
+        int jlo = max(ceil_small((lo - fx0) * inv_dx), left);
+        int jhi = min(floor_small((hi - fx0) * inv_dx), right - 1);
         // strictly inside: drop an end node that sits on the boundary
-        if (jlo <= jhi && fx0 + (float)jlo * dx <= lo) ++jlo;
-        if (jlo <= jhi && fx0 + (float)jhi * dx >= hi) --jhi;
-        int glo = jlo + f.coff, ghi = jhi + f.coff;
+        if (jlo <= jhi && fx0 + i2f_small(jlo) * dx <= lo) ++jlo;
+        if (jlo <= jhi && fx0 + i2f_small(jhi) * dx >= hi) --jhi;
+        int glo = jlo + coff, ghi = jhi + coff;
         glo = glo < 0 ? 0 : glo;
         ghi = ghi >= gncols ? gncols - 1 : ghi;
         if (glo > ghi) continue;
@@ -180,206 +211,371 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     }
 }
 
-template <bool CONFINED>
-__device__ __forceinline__ void trace32(const TrackLaunch& L, int r, int p, long long idx, const float4* sm32,
-                                        const Chron& ch);
 
+// Dormand-Prince tableau in FP32 (capturezone.py:202-209), arranged for
+// running sums.  Row s = 0..5 is the stage point of k_{s+2} (row 5 is the
+// 5th-order solution).  After k_{j+1} (j = 0..5) is evaluated it is added
+// into every later row: P_s += c_dp_b[j][s] * k, where c_dp_b[j][s] is
+// a[s][j+1] for s > j and 0 otherwise, and into the error sum with
+// c_dp_e[j+1] (k7 = f(xyt) carries -1/40, the reference's e[1]).
+__constant__ float c_dp_a0[6] = {(float)DP::a2, (float)DP::a31, (float)DP::a41, (float)DP::a51,
+                                 (float)DP::a61, (float)DP::a71};
+__constant__ float c_dp_b[6][6] = {
+    {0, (float)DP::a32, (float)DP::a42, (float)DP::a52, (float)DP::a62, 0.0f},
+    {0, 0, (float)DP::a43, (float)DP::a53, (float)DP::a63, (float)DP::a73},
+    {0, 0, 0, (float)DP::a54, (float)DP::a64, (float)DP::a74},
+    {0, 0, 0, 0, (float)DP::a65, (float)DP::a75},
+    {0, 0, 0, 0, 0, (float)DP::a76},
+    {0, 0, 0, 0, 0, 0}};
+__constant__ float c_dp_e[7] = {(float)DP::e1, 0.0f, (float)DP::e3, (float)DP::e4, (float)DP::e5,
+                                (float)DP::e6, (float)DP::e2};
+
+struct RealConst32 {
+    float c0, c1, c2, c3, c4, c5, K, n, H, inv_hn, ox, oy, kh2f, inv_k, inv_kh;
+    float tol, maxstep, dx, dy, umbra;   // options, converted once
+    int skip;
+    int next;            // next particle of this block's chunk
+};
+
+// Per-lane particle state.  Everything the step loop touches is FP32: on
+// GB300 the FP64 pipe runs at ~1/64 of the FP32 rate, so a handful of FP64
+// operations per step would dominate it.  The time left is a float pair
+// (tau_h + tau_l, error-free updates), counting down to zero.  Only what
+// every attempt reads stays in registers; the rest of a particle's state
+// (read or written once per accepted step at most) sits in shared memory,
+// one column per lane, so more lanes fit on an SM.
+struct Particle32 {
+    int p;               // particle index, >= pend when the lane is out of work
+    int status, att;
+    float tau_h, tau_l;  // duration - t
+    float dt, xh, xl, yh, yl;
+    float k1x, k1y;      // f at the current point (first stage, FSAL)
+};
+
+// Shared-memory columns of the per-lane cold state: field f of lane t at
+// cold[f * BLOCK + t] (conflict-free).
+enum ColdField { kNv, kAcc, kRlo, kRhi, kNtest, kNatom, kBx0, kBx1, kBy0, kBy1, kFx0, kFy0, kCoff,
+                 kRoff, kNcols, kNrows, kColdFields };
+
+template <int BLOCK>
+struct Cold {
+    uint32_t* base;
+    __device__ __forceinline__ int& i(ColdField f) const {
+        return reinterpret_cast<int*>(base)[f * BLOCK + threadIdx.x];
+    }
+    __device__ __forceinline__ float& f(ColdField fld) const {
+        return reinterpret_cast<float*>(base)[fld * BLOCK + threadIdx.x];
+    }
+};
+
+// The realization's constants, re-read from shared memory at every velocity
+// evaluation (a broadcast load) rather than held in registers.
 template <bool CONFINED>
-__global__ void __launch_bounds__(256) track32_kernel(const TrackLaunch L) {
+__device__ __forceinline__ bool feval_c(const RealConst32& rc_, const float4* w, int nw, float x, float y,
+                                        float& kx, float& ky) {
+    const volatile RealConst32& rc = rc_;
+    Model32 m;
+    m.w = w;
+    m.nw = nw;
+    m.ox = rc.ox; m.oy = rc.oy;
+    m.c0 = rc.c0; m.c1 = rc.c1; m.c2 = rc.c2; m.c3 = rc.c3; m.c4 = rc.c4; m.c5 = rc.c5;
+    m.K = rc.K; m.n = rc.n; m.H = rc.H; m.inv_hn = rc.inv_hn; m.kh2f = rc.kh2f;
+    m.inv_k = rc.inv_k; m.inv_kh = rc.inv_kh;
+    return feval32<CONFINED>(m, x, y, kx, ky);
+}
+
+// Write the finished particle's outputs.
+template <int BLOCK>
+__device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Particle32& s, const Cold<BLOCK>& c,
+                                         const Chron& ch) {
+    const long long idx = (long long)r * L.npaths + s.p;
+    if (L.out.endpoint) {
+        L.out.endpoint[2 * idx] = L.xt + ((double)s.xh + (double)s.xl);
+        L.out.endpoint[2 * idx + 1] = L.yt + ((double)s.yh + (double)s.yl);
+    }
+    if (L.out.bbox) {
+        L.out.bbox[4 * idx] = L.xt + (double)c.f(kBx0);
+        L.out.bbox[4 * idx + 1] = L.xt + (double)c.f(kBx1);
+        L.out.bbox[4 * idx + 2] = L.yt + (double)c.f(kBy0);
+        L.out.bbox[4 * idx + 3] = L.yt + (double)c.f(kBy1);
+    }
+    if (L.out.naccept) L.out.naccept[idx] = c.i(kAcc);
+    if (L.out.nattempt) L.out.nattempt[idx] = s.att;
+    if (L.out.status) L.out.status[idx] = s.status;
+    if (L.out.nvertices) L.out.nvertices[idx] = c.i(kNv);
+    note_rows(ch.slot, L.mask_words, L.grid.nrows, c.i(kRlo), c.i(kRhi));
+    add_counters((long long*)L.out.counters, s.att, c.i(kAcc), (unsigned)c.i(kNtest), (unsigned)c.i(kNatom));
+}
+
+template <int BLOCK>
+__device__ __forceinline__ void push_vertex(const TrackLaunch& L, int r, const Particle32& s, const Cold<BLOCK>& c) {
+    const int nv = c.i(kNv);
+    if (L.out.vertices && nv < L.out.max_vertices) {
+        double* v = L.out.vertices + ((long long)r * L.npaths + s.p) * 2LL * L.out.max_vertices;
+        v[2 * nv] = L.xt + ((double)s.xh + (double)s.xl);
+        v[2 * nv + 1] = L.yt + ((double)s.yh + (double)s.yl);
+    }
+    c.i(kNv) = nv + 1;
+}
+
+// Start particle s.p: release point, frame, first velocity (k1).  Returns
+// false when the trace is already over (dry at the release point, or a zero
+// duration).
+template <bool CONFINED, int BLOCK>
+__device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealConst32& rc, const float4* w,
+                                        Particle32& s, const Cold<BLOCK>& c) {
+    const double rx = L.release[2 * s.p] - L.xt, ry = L.release[2 * s.p + 1] - L.yt;
+    s.xh = (float)rx;
+    s.yh = (float)ry;
+    s.xl = (float)(rx - (double)s.xh);
+    s.yl = (float)(ry - (double)s.yh);
+    const OnekaFrame f = frame_of(L, r, s.p);
+    c.f(kFx0) = (float)(f.xmin - L.xt);
+    c.f(kFy0) = (float)(f.ymin - L.yt);
+    c.i(kCoff) = f.coff;
+    c.i(kRoff) = f.roff;
+    c.i(kNcols) = f.ncols;
+    c.i(kNrows) = f.nrows;
+    s.status = ONEKA_TRACE_OK;
+    s.att = 0;
+    c.i(kAcc) = 0;
+    c.i(kNv) = 0;
+    c.i(kRlo) = 0x7fffffff;
+    c.i(kRhi) = -1;
+    c.i(kNtest) = 0;
+    c.i(kNatom) = 0;
+    const double dur = L.opts.duration;
+    s.tau_h = (float)dur;
+    s.tau_l = (float)(dur - (double)s.tau_h);
+    s.dt = 0.1f * (dur > 0.0 ? 1.0f : (dur < 0.0 ? -1.0f : 0.0f));
+    c.f(kBx0) = c.f(kBx1) = s.xh + s.xl;
+    c.f(kBy0) = c.f(kBy1) = s.yh + s.yl;
+    push_vertex<BLOCK>(L, r, s, c);
+    float kx, ky;
+    if (!feval_c<CONFINED>(rc, w, L.nwells, s.xh + s.xl, s.yh + s.yl, kx, ky)) {
+        s.status = ONEKA_TRACE_DRY;
+        return false;
+    }
+    s.k1x = kx;
+    s.k1y = ky;
+    return s.tau_h != 0.0f;
+}
+
+// One step attempt of the Dormand-Prince integrator (capturezone.py:221-247).
+// Returns false when the trace is over.
+template <bool CONFINED, int BLOCK>
+__device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst32& rc, const float4* w,
+                                          const Chron& ch, Particle32& s, int r, const Cold<BLOCK>& c) {
+    if (s.att >= L.max_attempts) {
+        s.status = ONEKA_TRACE_STEP_LIMIT;
+        return false;
+    }
+    ++s.att;
+    // do not step past the duration (capturezone.py:223-224): |dt| > |time left|
+    const float tau = s.tau_h + s.tau_l;
+    bool last = false;
+    if (fabsf(s.dt) > fabsf(tau)) {
+        s.dt = tau;
+        last = true;
+    }
+    const float dt = s.dt;
+    // running sums of the stage rows and of the error row, seeded with k1
+    float px[6], py[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        px[q] = c_dp_a0[q] * s.k1x;
+        py[q] = c_dp_a0[q] * s.k1y;
+    }
+    float ex = c_dp_e[0] * s.k1x, ey = c_dp_e[0] * s.k1y;
+    float kx = 0.0f, ky = 0.0f;
+#pragma unroll 1
+    for (int st = 0; st < 6; ++st) {            // evaluates k2..k7
+        // px[st] selected with compile-time indexes only
+        float ax = px[0], ay = py[0];
+#pragma unroll
+        for (int q = 1; q < 6; ++q)
+            if (q == st) { ax = px[q]; ay = py[q]; }
+        if (!feval_c<CONFINED>(rc, w, L.nwells, s.xh + (s.xl + dt * ax), s.yh + (s.yl + dt * ay), kx, ky)) {
+            s.status = ONEKA_TRACE_DRY;
+            return false;
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            px[q] += c_dp_b[st][q] * kx;
+            py[q] += c_dp_b[st][q] * ky;
+        }
+        ex += c_dp_e[st + 1] * kx;
+        ey += c_dp_e[st + 1] * ky;
+    }
+    // kx, ky = k7 = f(xyt); the 5th-order step is dt * P_5
+    const float sx = dt * px[5], sy = dt * py[5];
+    const float est = fmaxf(fabsf(dt * ex), fabsf(dt * ey));
+    const float ds = sqrtf(sx * sx + sy * sy);
+    const float tol = rc.tol, maxstep = rc.maxstep, eps = (float)DP::eps;
+    if ((est < tol) && (ds < maxstep)) {
+        if (last) {
+            s.tau_h = s.tau_l = 0.0f;
+        } else {
+            float th, te;
+            two_sum(s.tau_h, -dt, th, te);
+            te += s.tau_l;
+            two_sum(th, te, s.tau_h, s.tau_l);
+        }
+        const float ax = s.xh + s.xl, ay = s.yh + s.yl;
+        float q, e;
+        two_sum(s.xh, sx, q, e);
+        s.xl += e;
+        two_sum(q, s.xl, s.xh, e);
+        s.xl = e;
+        two_sum(s.yh, sy, q, e);
+        s.yl += e;
+        two_sum(q, s.yl, s.yh, e);
+        s.yl = e;
+        const float bxn = s.xh + s.xl, byn = s.yh + s.yl;
+        if (ch.slot) {
+            long long ntest = (unsigned)c.i(kNtest), natom = (unsigned)c.i(kNatom);
+            int rlo = c.i(kRlo), rhi = c.i(kRhi);
+            insert32(ch, L.grid.nrows, L.grid.ncols, c.i(kCoff), c.i(kRoff), c.i(kNcols), c.i(kNrows),
+                     c.f(kFx0), c.f(kFy0), rc.dx, rc.dy, rc.umbra, ax, ay,
+                     bxn, byn, ntest, natom, rlo, rhi);
+            c.i(kNtest) = (int)ntest;
+            c.i(kNatom) = (int)natom;
+            c.i(kRlo) = rlo;
+            c.i(kRhi) = rhi;
+        }
+        c.f(kBx0) = fminf(c.f(kBx0), bxn); c.f(kBx1) = fmaxf(c.f(kBx1), bxn);
+        c.f(kBy0) = fminf(c.f(kBy0), byn); c.f(kBy1) = fmaxf(c.f(kBy1), byn);
+        s.k1x = kx;
+        s.k1y = ky;
+        push_vertex<BLOCK>(L, r, s, c);
+        c.i(kAcc) += 1;
+    }
+    float fac = __powf(tol / (est + eps), 0.2f);
+    const float fstep = maxstep / (ds + eps);
+    if (fstep < fac) fac = fstep;
+    if (10.0f < fac) fac = 10.0f;
+    s.dt = 0.9f * fac * dt;
+    return s.tau_h != 0.0f;
+}
+
+template <bool CONFINED, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) track32_kernel(const TrackLaunch L, int chunks) {
     extern __shared__ float4 sm32[];
+    __shared__ RealConst32 rc;
     const int k = blockIdx.y;
     const int r = L.r0 + k;
+    float4* w = sm32;
+    Cold<BLOCK> cold;
+    cold.base = reinterpret_cast<uint32_t*>(sm32 + L.nwells);
     uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
-    const Chron ch = make_chron(L, slot, reinterpret_cast<uint32_t*>(sm32 + L.nwells));
-    for (int i = threadIdx.x; i < L.nwells; i += blockDim.x) {
+    const Chron ch = make_chron(L, slot, cold.base + kColdFields * BLOCK);
+    // particles [pbeg, pend) of this block
+    const int per = (L.npaths + chunks - 1) / chunks;
+    const int pbeg = blockIdx.x * per;
+    const int pend = min(L.npaths, pbeg + per);
+    if (threadIdx.x == 0) {
+        const double* c = L.coef + 6LL * r;
+        const double Kd = L.aquifer[3LL * r], nd = L.aquifer[3LL * r + 1], Hd = L.aquifer[3LL * r + 2];
+        rc.c0 = (float)c[0]; rc.c1 = (float)c[1]; rc.c2 = (float)c[2];
+        rc.c3 = (float)c[3]; rc.c4 = (float)c[4]; rc.c5 = (float)c[5];
+        rc.K = (float)Kd; rc.n = (float)nd; rc.H = (float)Hd;
+        rc.inv_hn = (float)(1.0 / (Hd * nd));
+        rc.kh2f = (float)(0.5 * Kd * (Hd * Hd));
+        rc.inv_k = (float)(1.0 / Kd);
+        rc.inv_kh = (float)(1.0 / (Kd * Hd));
+        rc.tol = (float)L.opts.tol;
+        rc.maxstep = (float)L.opts.maxstep;
+        rc.dx = (float)L.grid.dx;
+        rc.dy = (float)L.grid.dy;
+        rc.umbra = (float)L.opts.umbra;
+        rc.ox = (float)(L.xo - L.xt);
+        rc.oy = (float)(L.yo - L.yt);
+        rc.skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
+        rc.next = pbeg + BLOCK;
+        if (!rc.skip && blockIdx.x == 0 && L.registered) atomicAdd(L.registered, 1ull);
+    }
+    for (int i = threadIdx.x; i < L.nwells; i += BLOCK) {
         const double q = L.q[(long long)r * L.nwells + i];
-        sm32[i] = make_float4((float)(L.wells[3 * i] - L.xt), (float)(L.wells[3 * i + 1] - L.yt),
-                              (float)(-q * 0.15915494309189535), (float)(q * 0.07957747154594767));
+        w[i] = make_float4((float)(L.wells[3 * i] - L.xt), (float)(L.wells[3 * i + 1] - L.yt),
+                           (float)(-q * 0.15915494309189535), (float)(q * 0.07957747154594767));
     }
     window_clear(ch);
     __syncthreads();
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const long long idx = (long long)r * L.npaths + p;
-    const bool skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
-    if (!skip && blockIdx.x == 0 && threadIdx.x == 0 && L.registered) atomicAdd(L.registered, 1ull);
-    if (p < L.npaths) {
-        if (skip) {
-            if (L.out.status) L.out.status[idx] = kTraceSkipped;
-        } else {
-            trace32<CONFINED>(L, r, p, idx, sm32, ch);
+    if (rc.skip) {
+        if (L.out.status)
+            for (int p = pbeg + threadIdx.x; p < pend; p += BLOCK)
+                L.out.status[(long long)r * L.npaths + p] = kTraceSkipped;
+        return;   // uniform across the block: nothing was marked
+    }
+    Particle32 s;
+    s.p = pbeg + threadIdx.x;
+    bool live = false;
+    // start this lane's first particle; a lane whose trace ends at once takes the next
+    while (s.p < pend && !live) {
+        live = start32<CONFINED, BLOCK>(L, r, rc, w, s, cold);
+        if (!live) {
+            finish32<BLOCK>(L, r, s, cold, ch);
+            s.p = atomicAdd(&rc.next, 1);
+        }
+    }
+    while (live) {
+        live = attempt32<CONFINED, BLOCK>(L, rc, w, ch, s, r, cold);
+        while (!live && s.p < pend) {
+            finish32<BLOCK>(L, r, s, cold, ch);
+            s.p = atomicAdd(&rc.next, 1);
+            if (s.p < pend) live = start32<CONFINED, BLOCK>(L, r, rc, w, s, cold);
         }
     }
     __syncthreads();
     window_flush(ch);
 }
 
+template <bool CONFINED, int BLOCK, int MINB>
+cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    // split realizations into particle chunks only when they cannot fill the GPU
+    const int target = 2 * sms * MINB;
+    int chunks = 1;
+    if (L.nr < target) {
+        chunks = (target + L.nr - 1) / L.nr;
+        const int maxc = (L.npaths + BLOCK - 1) / BLOCK;
+        if (chunks > maxc) chunks = maxc;
+        if (chunks < 1) chunks = 1;
+    }
+    const size_t smem = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)kColdFields * BLOCK +
+                        4 * (size_t)L.win_rows * L.win_words;
+    auto kern = track32_kernel<CONFINED, BLOCK, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<dim3((unsigned)chunks, (unsigned)L.nr), BLOCK, smem, s>>>(L, chunks);
+    return cudaGetLastError();
+}
+
 template <bool CONFINED>
-__device__ __forceinline__ void trace32(const TrackLaunch& L, int r, int p, long long idx, const float4* sm32,
-                                        const Chron& ch) {
-
-    Model32 m;
-    m.w = sm32;
-    m.nw = L.nwells;
-    m.ox = (float)(L.xo - L.xt);
-    m.oy = (float)(L.yo - L.yt);
-    const double* c = L.coef + 6LL * r;
-    m.c0 = (float)c[0]; m.c1 = (float)c[1]; m.c2 = (float)c[2];
-    m.c3 = (float)c[3]; m.c4 = (float)c[4]; m.c5 = (float)c[5];
-    const double Kd = L.aquifer[3LL * r], nd = L.aquifer[3LL * r + 1], Hd = L.aquifer[3LL * r + 2];
-    m.K = (float)Kd;
-    m.n = (float)nd;
-    m.H = (float)Hd;
-    m.inv_hn = (float)(1.0 / (Hd * nd));
-    m.kh2 = 0.5 * Kd * (Hd * Hd);
-
-    const OnekaFrame f = frame_of(L, r, p);
-    const float fx0 = (float)(f.xmin - L.xt);
-    const float fy0 = (float)(f.ymin - L.yt);
-    uint32_t* slot = ch.slot;
-    const float gdx = (float)L.grid.dx, gdy = (float)L.grid.dy, umbra = (float)L.opts.umbra;
-
-    const double dur = L.opts.duration;
-    const float tol = (float)L.opts.tol;
-    const float maxstep = (float)L.opts.maxstep;
-    const float eps = (float)DP::eps;
-    double t = 0.0;
-    float dt = 0.1f * (dur > 0.0 ? 1.0f : (dur < 0.0 ? -1.0f : 0.0f));
-    float xh = (float)(L.release[2 * p] - L.xt), yh = (float)(L.release[2 * p + 1] - L.yt);
-    float xl = (float)((L.release[2 * p] - L.xt) - (double)xh);
-    float yl = (float)((L.release[2 * p + 1] - L.yt) - (double)yh);
-
-    double* vout = L.out.vertices ? L.out.vertices + idx * 2LL * L.out.max_vertices : nullptr;
-    int nv = 0;
-    float bx0 = xh + xl, bx1 = bx0, by0 = yh + yl, by1 = by0;
-    auto push = [&](float ph, float pl, float qh, float ql) {
-        if (vout && nv < L.out.max_vertices) {
-            vout[2 * nv] = L.xt + ((double)ph + (double)pl);
-            vout[2 * nv + 1] = L.yt + ((double)qh + (double)ql);
-        }
-        ++nv;
-    };
-    push(xh, xl, yh, yl);
-
-    int status = ONEKA_TRACE_OK;
-    int acc = 0, att = 0;
-    long long ntest = 0, natom = 0;
-    int rlo = 0x7fffffff, rhi = -1;
-    float k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y, k5x, k5y, k6x, k6y, k7x, k7y;
-    constexpr float a2 = (float)DP::a2, a31 = (float)DP::a31, a32 = (float)DP::a32;
-    constexpr float a41 = (float)DP::a41, a42 = (float)DP::a42, a43 = (float)DP::a43;
-    constexpr float a51 = (float)DP::a51, a52 = (float)DP::a52, a53 = (float)DP::a53, a54 = (float)DP::a54;
-    constexpr float a61 = (float)DP::a61, a62 = (float)DP::a62, a63 = (float)DP::a63, a64 = (float)DP::a64,
-                    a65 = (float)DP::a65;
-    constexpr float a71 = (float)DP::a71, a73 = (float)DP::a73, a74 = (float)DP::a74, a75 = (float)DP::a75,
-                    a76 = (float)DP::a76;
-    constexpr float e1 = (float)DP::e1, e2 = (float)DP::e2, e3 = (float)DP::e3, e4 = (float)DP::e4,
-                    e5 = (float)DP::e5, e6 = (float)DP::e6;
-    if (!feval32<CONFINED>(m, xh + xl, yh + yl, k1x, k1y)) {
-        status = ONEKA_TRACE_DRY;
-    } else {
-        while (fabs(t) < fabs(dur)) {
-            if (att >= L.max_attempts) {
-                status = ONEKA_TRACE_STEP_LIMIT;
-                break;
-            }
-            ++att;
-            bool last = false;
-            if (fabs(t + (double)dt) > fabs(dur)) {
-                dt = (float)(dur - t);
-                last = true;
-            }
-            if (!feval32<CONFINED>(m, xh + (xl + dt * (a2 * k1x)), yh + (yl + dt * (a2 * k1y)), k2x, k2y)) {
-                status = ONEKA_TRACE_DRY; break;
-            }
-            if (!feval32<CONFINED>(m, xh + (xl + dt * (a31 * k1x + a32 * k2x)),
-                                   yh + (yl + dt * (a31 * k1y + a32 * k2y)), k3x, k3y)) {
-                status = ONEKA_TRACE_DRY; break;
-            }
-            if (!feval32<CONFINED>(m, xh + (xl + dt * (a41 * k1x + a42 * k2x + a43 * k3x)),
-                                   yh + (yl + dt * (a41 * k1y + a42 * k2y + a43 * k3y)), k4x, k4y)) {
-                status = ONEKA_TRACE_DRY; break;
-            }
-            if (!feval32<CONFINED>(m, xh + (xl + dt * (a51 * k1x + a52 * k2x + a53 * k3x + a54 * k4x)),
-                                   yh + (yl + dt * (a51 * k1y + a52 * k2y + a53 * k3y + a54 * k4y)), k5x, k5y)) {
-                status = ONEKA_TRACE_DRY; break;
-            }
-            if (!feval32<CONFINED>(m, xh + (xl + dt * (a61 * k1x + a62 * k2x + a63 * k3x + a64 * k4x + a65 * k5x)),
-                                   yh + (yl + dt * (a61 * k1y + a62 * k2y + a63 * k3y + a64 * k4y + a65 * k5y)),
-                                   k6x, k6y)) {
-                status = ONEKA_TRACE_DRY; break;
-            }
-            const float sx = dt * (a71 * k1x + a73 * k3x + a74 * k4x + a75 * k5x + a76 * k6x);
-            const float sy = dt * (a71 * k1y + a73 * k3y + a74 * k4y + a75 * k5y + a76 * k6y);
-            if (!feval32<CONFINED>(m, xh + (xl + sx), yh + (yl + sy), k7x, k7y)) {
-                status = ONEKA_TRACE_DRY; break;
-            }
-            const float ex = dt * (e1 * k1x + e2 * k7x + e3 * k3x + e4 * k4x + e5 * k5x + e6 * k6x);
-            const float ey = dt * (e1 * k1y + e2 * k7y + e3 * k3y + e4 * k4y + e5 * k5y + e6 * k6y);
-            const float est = fmaxf(fabsf(ex), fabsf(ey));
-            const float ds = sqrtf(sx * sx + sy * sy);
-            if ((est < tol) && (ds < maxstep)) {
-                t = last ? dur : t + (double)dt;
-                const float ax = xh + xl, ay = yh + yl;
-                float s, e;
-                two_sum(xh, sx, s, e);
-                xl += e;
-                two_sum(s, xl, xh, e);
-                xl = e;
-                two_sum(yh, sy, s, e);
-                yl += e;
-                two_sum(s, yl, yh, e);
-                yl = e;
-                const float bxn = xh + xl, byn = yh + yl;
-                if (slot)
-                    insert32(ch, L.grid.nrows, L.grid.ncols, f, fx0, fy0, gdx, gdy, umbra,
-                             ax, ay, bxn, byn, ntest, natom, rlo, rhi);
-                bx0 = fminf(bx0, bxn); bx1 = fmaxf(bx1, bxn);
-                by0 = fminf(by0, byn); by1 = fmaxf(by1, byn);
-                k1x = k7x;
-                k1y = k7y;
-                push(xh, xl, yh, yl);
-                ++acc;
-            }
-            float fac = __powf(tol / (est + eps), 0.2f);
-            const float fstep = maxstep / (ds + eps);
-            if (fstep < fac) fac = fstep;
-            if (10.0f < fac) fac = 10.0f;
-            dt = 0.9f * fac * dt;
-        }
-    }
-    if (L.out.endpoint) {
-        L.out.endpoint[2 * idx] = L.xt + ((double)xh + (double)xl);
-        L.out.endpoint[2 * idx + 1] = L.yt + ((double)yh + (double)yl);
-    }
-    if (L.out.bbox) {
-        L.out.bbox[4 * idx] = L.xt + (double)bx0;
-        L.out.bbox[4 * idx + 1] = L.xt + (double)bx1;
-        L.out.bbox[4 * idx + 2] = L.yt + (double)by0;
-        L.out.bbox[4 * idx + 3] = L.yt + (double)by1;
-    }
-    if (L.out.naccept) L.out.naccept[idx] = acc;
-    if (L.out.nattempt) L.out.nattempt[idx] = att;
-    if (L.out.status) L.out.status[idx] = status;
-    if (L.out.nvertices) L.out.nvertices[idx] = nv;
-    note_rows(slot, L.mask_words, L.grid.nrows, rlo, rhi);
-    add_counters((long long*)L.out.counters, att, acc, ntest, natom);
+cudaError_t launch_confined(const TrackLaunch& L, cudaStream_t s) {
+    // (threads per block, minimum resident blocks per SM): the variants the
+    // autotuner chooses between through OnekaTrackOpts.block / .occupancy
+    const int block = L.opts.block > 0 ? L.opts.block : 128;
+    const int occ = L.opts.occupancy;
+    if (block == 64) return launch_variant<CONFINED, 64, 8>(L, s);
+    if (block == 256) return occ >= 3 ? launch_variant<CONFINED, 256, 3>(L, s)
+                                      : launch_variant<CONFINED, 256, 2>(L, s);
+    if (block == 32) return launch_variant<CONFINED, 32, 16>(L, s);
+    if (occ >= 8) return launch_variant<CONFINED, 128, 8>(L, s);
+    if (occ >= 6) return launch_variant<CONFINED, 128, 6>(L, s);
+    return launch_variant<CONFINED, 128, 4>(L, s);
 }
 
 }  // namespace
 
 cudaError_t launch_track32(const TrackLaunch& L, cudaStream_t s) {
-    const int block = L.opts.block > 0 ? L.opts.block : 128;
-    dim3 grid((unsigned)((L.npaths + block - 1) / block), (unsigned)L.nr);
-    if (grid.x == 0) grid.x = 1;
-    const size_t smem = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)L.win_rows * L.win_words;
-    if (L.opts.confined) {
-        cudaFuncSetAttribute(track32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        track32_kernel<true><<<grid, block, smem, s>>>(L);
-    } else {
-        cudaFuncSetAttribute(track32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        track32_kernel<false><<<grid, block, smem, s>>>(L);
-    }
-    return cudaGetLastError();
+    return L.opts.confined ? launch_confined<true>(L, s) : launch_confined<false>(L, s);
 }
 
 }  // namespace oneka

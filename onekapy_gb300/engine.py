@@ -284,11 +284,13 @@ class TrackOptions:
     max_attempts: int = 0
     block: int = 0
     window_kb: int = 0
+    occupancy: int = 0
 
     def c(self) -> C.OnekaTrackOpts:
         return C.OnekaTrackOpts(float(self.duration), float(self.tol), float(self.maxstep),
                                 float(self.umbra), int(bool(self.confined)), int(self.precision),
-                                int(self.max_attempts), int(self.block), int(self.window_kb), 0)
+                                int(self.max_attempts), int(self.block), int(self.window_kb),
+                                int(self.occupancy))
 
 
 @dataclass
