@@ -217,6 +217,9 @@ def run_ours(a):
                                      umbra=spec.umbra, confined=spec.confined, precision=prec)
     o32, o64 = mk(C.FP32), mk(C.FP64)
     stream = torch.cuda.current_stream()
+    # block shape / occupancy / chronicle window picked on a sample (setup, untimed)
+    E.realize(site, R, seed=SEED, first=first, out=real)
+    o32 = E.autotune(site, real, release, o32, grid, sample=min(R, 1024))
 
     def step(opts, n, ev=None, outputs=None):
         counts.zero_()
@@ -341,6 +344,8 @@ def run_ours(a):
                              "peak_source": "measured FP32 FMA loop on this GPU (oneka_fma_peak)"},
                 "e2e": {"value": e2e_n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
+                "tracker_launch": {"block": o32.block, "occupancy": o32.occupancy,
+                                   "window_kb": o32.window_kb, "chosen_by": "autotune on 1024 realizations"},
                 "gpu_launches": 3 * a.steps,
                 "clocks": clocks,
                 "cpu_baseline": cpu}

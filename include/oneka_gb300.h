@@ -128,10 +128,10 @@ typedef struct OnekaTrackOpts {
     int32_t confined;        /* 1: compute_velocity_confined; 0: compute_velocity */
     int32_t precision;       /* ONEKA_FP64 or ONEKA_FP32 */
     int32_t max_attempts;    /* step attempts per particle before STEP_LIMIT; <= 0: 1,000,000 */
-    int32_t block;           /* threads per block: 32, 64, 128 or 256; 0: 128 */
+    int32_t block;           /* threads per block: 32, 64, 128 or 256; 0: 256 (FP32), 128 (FP64) */
     int32_t window_kb;       /* shared-memory chronicle window per block in KiB (0: 32; < 0: none) */
     int32_t occupancy;       /* FP32 build: resident blocks per SM to compile for (4, 6, 8 at 128
-                                threads; 2, 3 at 256); 0: 4 */
+                                threads; 2, 3 at 256); 0: the lowest */
 } OnekaTrackOpts;
 
 /* Optional per-particle outputs ([nreal][npaths] leading); any pointer may be NULL. */
@@ -210,6 +210,35 @@ ONEKA_API int oneka_track(const OnekaSite* site, const OnekaRealizations* real, 
                 const OnekaGrid* grid, const OnekaFrame* frames, int32_t* counts,
                 int64_t* registered, const OnekaTrackOut* out, void* scratch,
                 size_t scratch_bytes, void* stream);
+
+/* One site of a batched launch (oneka_track_batched); pointers to structs are host pointers. */
+typedef struct OnekaTrackJob {
+    const OnekaSite* site;
+    const OnekaRealizations* real;
+    int32_t nreal, npaths;
+    const double* release;           /* device [npaths][2] */
+    const OnekaTrackOpts* opts;      /* precision must be ONEKA_FP32; block/occupancy of job 0 apply to all */
+    const OnekaGrid* grid;
+    int32_t* counts;                 /* device [nrows][ncols] int32 */
+    int64_t* registered;             /* device, may be NULL */
+    const OnekaTrackOut* out;        /* may be NULL */
+} OnekaTrackJob;
+
+/* Scratch bytes oneka_track_batched needs to run every realization of the jobs in one wave. */
+ONEKA_API size_t oneka_track_batched_scratch_bytes(const OnekaTrackJob* jobs, int32_t njobs);
+
+/*
+ * Many sites in one launch (FP32 build): every realization of every job --
+ * sites with uneven well counts, npaths, durations, grids, confined or not --
+ * is a block row of one persistent tracking kernel whose lanes refill from
+ * their realization's particles, followed by one register kernel.  Rows are
+ * packed into waves that fit `scratch` (zero on entry, zero on return, like
+ * oneka_track).  Up to 80 jobs form one launch; more jobs run as further
+ * launches.  Each job's semantics are those of oneka_track with the same
+ * arguments.  No host synchronization; capturable in a CUDA graph.
+ */
+ONEKA_API int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void* scratch,
+                                  size_t scratch_bytes, void* stream);
 
 /* Size of the fixed scratch array inside the library that oneka_track_noalloc uses. */
 #define ONEKA_NOALLOC_SCRATCH_BYTES (32u << 20)

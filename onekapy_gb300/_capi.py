@@ -25,7 +25,7 @@ FP64, FP32 = 0, 1
 EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_realize",
            "oneka_track_scratch_bytes", "oneka_track", "oneka_evaluate", "oneka_rasterize",
            "oneka_register_weighted", "oneka_distancesquared", "oneka_fma_peak",
-           "oneka_track_noalloc"]
+           "oneka_track_noalloc", "oneka_track_batched", "oneka_track_batched_scratch_bytes"]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
@@ -68,6 +68,13 @@ class OnekaTrackOut(ctypes.Structure):
                 ("counters", _P)]
 
 
+class OnekaTrackJob(ctypes.Structure):
+    _fields_ = [("site", ctypes.POINTER(OnekaSite)), ("real", ctypes.POINTER(OnekaRealizations)),
+                ("nreal", _I), ("npaths", _I), ("release", _P), ("opts", ctypes.POINTER(OnekaTrackOpts)),
+                ("grid", ctypes.POINTER(OnekaGrid)), ("counts", _P), ("registered", _P),
+                ("out", ctypes.POINTER(OnekaTrackOut))]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -108,6 +115,10 @@ def load() -> ctypes.CDLL:
                                           _P, _I, ctypes.POINTER(OnekaTrackOpts),
                                           ctypes.POINTER(OnekaGrid), _P, _P, _P,
                                           ctypes.POINTER(OnekaTrackOut), _P]
+        L.oneka_track_batched_scratch_bytes.restype = ctypes.c_size_t
+        L.oneka_track_batched_scratch_bytes.argtypes = [ctypes.POINTER(OnekaTrackJob), _I]
+        L.oneka_track_batched.restype = ctypes.c_int
+        L.oneka_track_batched.argtypes = [ctypes.POINTER(OnekaTrackJob), _I, _P, ctypes.c_size_t, _P]
         L.oneka_evaluate.restype = ctypes.c_int
         L.oneka_evaluate.argtypes = [ctypes.POINTER(OnekaSite), _P, _D, _D, _D,
                                      ctypes.POINTER(ctypes.c_double), _P, ctypes.c_int64, _I, _P, _P,

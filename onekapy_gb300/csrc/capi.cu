@@ -1,6 +1,8 @@
 // capi.cu -- extern "C" entry points of liboneka_gb300.so (include/oneka_gb300.h).
 #include <math.h>
 #include <stdarg.h>
+
+#include <memory>
 #include <stdio.h>
 #include <string.h>
 
@@ -88,6 +90,57 @@ static void set_window(TrackLaunch& L, const OnekaGrid& g, int window_kb) {
     L.win_words = ww;
 }
 
+// Argument checks shared by oneka_track and oneka_track_batched.
+static int check_track_args(const OnekaSite* site, const OnekaRealizations* real, int32_t nreal,
+                            const double* release, int32_t npaths, const OnekaTrackOpts* opts,
+                            const OnekaGrid* grid, const OnekaTrackOut* out) {
+    ONEKA_CHECK_ARG(site && real && opts && grid, "site/real/opts/grid");
+    ONEKA_CHECK_ARG(grid_ok(grid), "grid (nrows, ncols, dx, dy must be > 0)");
+    ONEKA_CHECK_ARG(nreal >= 0 && npaths >= 0, "nreal/npaths");
+    ONEKA_CHECK_ARG(npaths == 0 || release, "release");
+    ONEKA_CHECK_ARG(site->nwells >= 1 && site->nwells <= 2048 && site->wells, "wells (1..2048)");
+    ONEKA_CHECK_ARG(site->target >= 0 && site->target < site->nwells, "target index");
+    ONEKA_CHECK_ARG(real->coef && real->q && real->aquifer, "realization arrays");
+    ONEKA_CHECK_ARG(opts->precision == ONEKA_FP64 || opts->precision == ONEKA_FP32, "precision");
+    ONEKA_CHECK_ARG(opts->tol > 0 && opts->maxstep > 0 && opts->umbra >= 0, "tol/maxstep/umbra");
+    ONEKA_CHECK_ARG(opts->block == 0 || opts->block == 32 || opts->block == 64 || opts->block == 128 ||
+                    opts->block == 256, "block must be 32, 64, 128 or 256");
+    ONEKA_CHECK_ARG(!out || out->max_vertices >= 0, "max_vertices");
+    ONEKA_CHECK_ARG(!out || !out->vertices || out->max_vertices > 0, "vertices without max_vertices");
+    return ONEKA_OK;
+}
+
+static void fill_launch(TrackLaunch& L, const OnekaSite* site, const OnekaRealizations* real,
+                        const double* release, int32_t npaths, const OnekaTrackOpts* opts,
+                        const OnekaGrid* grid, const OnekaFrame* frames, int64_t* registered,
+                        const OnekaTrackOut* out) {
+    memset(&L, 0, sizeof(L));
+    L.nwells = site->nwells;
+    L.npaths = npaths;
+    L.wells = site->wells;
+    L.xo = site->xo;
+    L.yo = site->yo;
+    // The regional origin anchors the FP32 build's relative coordinates (the
+    // stochastic driver puts it on the target well).
+    L.xt = site->xo;
+    L.yt = site->yo;
+    L.coef = real->coef;
+    L.q = real->q;
+    L.aquifer = real->aquifer;
+    L.rstatus = real->status;
+    L.release = release;
+    L.opts = *opts;
+    L.grid = *grid;
+    L.frames = frames;
+    L.wpr = words_per_row(grid->ncols);
+    L.slot_words = slot_words(*grid);
+    L.mask_words = mask_words(*grid);
+    L.registered = (unsigned long long*)registered;
+    if (out) L.out = *out;
+    L.max_attempts = opts->max_attempts > 0 ? opts->max_attempts : kDefaultMaxAttempts;
+    set_window(L, *grid, opts->window_kb);
+}
+
 extern "C" {
 
 int oneka_abi_version(void) { return ONEKA_ABI_VERSION; }
@@ -134,48 +187,13 @@ int oneka_track(const OnekaSite* site, const OnekaRealizations* real, int32_t nr
                 int64_t* registered, const OnekaTrackOut* out, void* scratch,
                 size_t scratch_bytes, void* stream) {
     g_err[0] = 0;
-    ONEKA_CHECK_ARG(site && real && opts && grid, "site/real/opts/grid");
-    ONEKA_CHECK_ARG(grid_ok(grid), "grid (nrows, ncols, dx, dy must be > 0)");
-    ONEKA_CHECK_ARG(nreal >= 0 && npaths >= 0, "nreal/npaths");
-    ONEKA_CHECK_ARG(npaths == 0 || release, "release");
-    ONEKA_CHECK_ARG(site->nwells >= 1 && site->nwells <= 2048 && site->wells, "wells (1..2048)");
-    ONEKA_CHECK_ARG(site->target >= 0 && site->target < site->nwells, "target index");
-    ONEKA_CHECK_ARG(real->coef && real->q && real->aquifer, "realization arrays");
-    ONEKA_CHECK_ARG(opts->precision == ONEKA_FP64 || opts->precision == ONEKA_FP32, "precision");
-    ONEKA_CHECK_ARG(opts->tol > 0 && opts->maxstep > 0 && opts->umbra >= 0, "tol/maxstep/umbra");
-    ONEKA_CHECK_ARG(opts->block == 0 || opts->block == 32 || opts->block == 64 || opts->block == 128 ||
-                    opts->block == 256, "block must be 32, 64, 128 or 256");
-    ONEKA_CHECK_ARG(!out || out->max_vertices >= 0, "max_vertices");
-    ONEKA_CHECK_ARG(!out || !out->vertices || out->max_vertices > 0, "vertices without max_vertices");
+    const int rc = check_track_args(site, real, nreal, release, npaths, opts, grid, out);
+    if (rc != ONEKA_OK) return rc;
     if (nreal == 0) return ONEKA_OK;
 
     cudaStream_t s = (cudaStream_t)stream;
     TrackLaunch L;
-    memset(&L, 0, sizeof(L));
-    L.nwells = site->nwells;
-    L.npaths = npaths;
-    L.wells = site->wells;
-    L.xo = site->xo;
-    L.yo = site->yo;
-    // The regional origin anchors the FP32 build's relative coordinates (the
-    // stochastic driver puts it on the target well).
-    L.xt = site->xo;
-    L.yt = site->yo;
-    L.coef = real->coef;
-    L.q = real->q;
-    L.aquifer = real->aquifer;
-    L.rstatus = real->status;
-    L.release = release;
-    L.opts = *opts;
-    L.grid = *grid;
-    L.frames = frames;
-    L.wpr = words_per_row(grid->ncols);
-    L.slot_words = slot_words(*grid);
-    L.mask_words = mask_words(*grid);
-    L.registered = (unsigned long long*)registered;
-    if (out) L.out = *out;
-    L.max_attempts = opts->max_attempts > 0 ? opts->max_attempts : kDefaultMaxAttempts;
-    set_window(L, *grid, opts->window_kb);
+    fill_launch(L, site, real, release, npaths, opts, grid, frames, registered, out);
 
     int wave = nreal < 65535 ? nreal : 65535;
     if (!counts && scratch) {
@@ -218,6 +236,84 @@ int oneka_track(const OnekaSite* site, const OnekaRealizations* real, int32_t nr
         if (counts) ONEKA_CHECK_CUDA(launch_register_counts(L.slots, L.nr, *grid, counts, s));
     }
     return ONEKA_OK;
+}
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+size_t oneka_track_batched_scratch_bytes(const OnekaTrackJob* jobs, int32_t njobs) {
+    if (!jobs || njobs < 0) return 0;
+    size_t total = 0;
+    for (int j = 0; j < njobs; ++j) {
+        if (!jobs[j].grid || !grid_ok(jobs[j].grid) || jobs[j].nreal < 0) return 0;
+        total += align256((size_t)slot_words(*jobs[j].grid) * 4u * (size_t)jobs[j].nreal);
+    }
+    return total;
+}
+
+int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void* scratch, size_t scratch_bytes,
+                        void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(jobs && njobs >= 0, "jobs");
+    ONEKA_CHECK_ARG(scratch && ((uintptr_t)scratch & 255u) == 0, "scratch must be 256-byte aligned");
+    for (int j = 0; j < njobs; ++j) {
+        const OnekaTrackJob& J = jobs[j];
+        const int rc = check_track_args(J.site, J.real, J.nreal, J.release, J.npaths, J.opts, J.grid, J.out);
+        if (rc != ONEKA_OK) return rc;
+        ONEKA_CHECK_ARG(J.opts->precision == ONEKA_FP32, "batched launches run the FP32 build");
+        ONEKA_CHECK_ARG(J.counts, "counts");
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    std::unique_ptr<JobTable> T(new JobTable());
+    int n = 0, rows = 0;
+    size_t off = 0;
+    auto flush = [&]() -> int {
+        if (n == 0) return ONEKA_OK;
+        T->first[n] = rows;
+        T->njobs = n;
+        ONEKA_CHECK_CUDA(launch_track32_batch(*T, rows, s));
+        ONEKA_CHECK_CUDA(launch_register_batch(*T, rows, s));
+        n = rows = 0;
+        off = 0;
+        return ONEKA_OK;
+    };
+    for (int j = 0; j < njobs; ++j) {
+        const OnekaTrackJob& J = jobs[j];
+        TrackLaunch base;
+        fill_launch(base, J.site, J.real, J.release, J.npaths, J.opts, J.grid, nullptr, J.registered, J.out);
+        base.counts = J.counts;
+        // every job shares job 0's launch shape
+        base.opts.block = jobs[0].opts->block;
+        base.opts.occupancy = jobs[0].opts->occupancy;
+        const size_t slot = (size_t)base.slot_words * 4u;
+        int r = 0;
+        while (r < J.nreal) {
+            const size_t room = off < scratch_bytes ? (scratch_bytes - off) / slot : 0;
+            if (room == 0 || n == kMaxJobs || rows == 65535) {
+                if (n == 0) {
+                    set_error("scratch of %zu bytes is smaller than one realization slot (%zu bytes)",
+                              scratch_bytes, slot);
+                    return ONEKA_ERR_SCRATCH;
+                }
+                const int rc = flush();
+                if (rc != ONEKA_OK) return rc;
+                continue;
+            }
+            int take = J.nreal - r;
+            if ((size_t)take > room) take = (int)room;
+            if (take > 65535 - rows) take = 65535 - rows;
+            TrackLaunch& L = T->job[n];
+            L = base;
+            L.r0 = r;
+            L.nr = take;
+            L.slots = (uint32_t*)((char*)scratch + off);
+            T->first[n] = rows;
+            ++n;
+            rows += take;
+            off = align256(off + (size_t)take * slot);
+            r += take;
+        }
+    }
+    return flush();
 }
 
 int oneka_evaluate(const OnekaSite* site, const double* q, double conductivity, double porosity,

@@ -16,11 +16,8 @@ namespace {
 // One block per realization slot: scan the rows its particles touched (the
 // slot header), add 1 to counts for every marked node, and clear the words
 // and the header as they are read (register() then rgrid[:] = False).
-__global__ void __launch_bounds__(256) register_counts_kernel(uint32_t* __restrict__ slots,
-                                                              long long slot_words, long long mask_words,
-                                                              int nrows, int ncols, int wpr,
-                                                              int32_t* __restrict__ counts) {
-    uint32_t* slot = slots + (long long)blockIdx.x * slot_words;
+__device__ __forceinline__ void register_slot(uint32_t* __restrict__ slot, long long mask_words, int nrows,
+                                              int ncols, int wpr, int32_t* __restrict__ counts) {
     const uint32_t h0 = slot[mask_words], h1 = slot[mask_words + 1];
     if (h1 == 0) return;
     // the header is written only by the tracker; clamping keeps a corrupted
@@ -46,6 +43,27 @@ __global__ void __launch_bounds__(256) register_counts_kernel(uint32_t* __restri
         slot[mask_words] = 0u;
         slot[mask_words + 1] = 0u;
     }
+}
+
+__global__ void __launch_bounds__(256) register_counts_kernel(uint32_t* __restrict__ slots,
+                                                              long long slot_words, long long mask_words,
+                                                              int nrows, int ncols, int wpr,
+                                                              int32_t* __restrict__ counts) {
+    register_slot(slots + (long long)blockIdx.x * slot_words, mask_words, nrows, ncols, wpr, counts);
+}
+
+// Register every slot of a batched launch: block row -> (job, realization).
+__global__ void __launch_bounds__(256) register_batch_kernel(const __grid_constant__ JobTable T) {
+    const int row = blockIdx.x;
+    int lo = 0, hi = T.njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (T.first[mid] <= row) lo = mid; else hi = mid - 1;
+    }
+    const TrackLaunch& J = T.job[lo];
+    if (!J.slots || !J.counts) return;
+    register_slot(J.slots + (long long)(row - T.first[lo]) * J.slot_words, J.mask_words, J.grid.nrows,
+                  J.grid.ncols, J.wpr, J.counts);
 }
 
 __global__ void register_weighted_kernel(uint32_t* __restrict__ mask, long long mwords, int nrows, int ncols,
@@ -169,6 +187,12 @@ cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid&
     if (nslots <= 0) return cudaSuccess;
     register_counts_kernel<<<(unsigned)nslots, 256, 0, s>>>(slots, slot_words(g), mask_words(g), g.nrows,
                                                             g.ncols, words_per_row(g.ncols), counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_register_batch(const JobTable& T, int rows, cudaStream_t s) {
+    if (rows <= 0) return cudaSuccess;
+    register_batch_kernel<<<(unsigned)rows, 256, 0, s>>>(T);
     return cudaGetLastError();
 }
 

@@ -38,7 +38,18 @@ struct TrackLaunch {
     // shared-memory window of each realization slot: rows [win_r0, win_r0 + win_rows),
     // words [win_w0, win_w0 + win_words) of every row; win_rows == 0: no window
     int win_r0, win_w0, win_rows, win_words;
+    int32_t* counts;            // register target of this launch (batched launches)
 };
+
+// The jobs of one batched launch (oneka_track_batched), passed whole as a
+// __grid_constant__ kernel parameter: first[j] is job j's first block row.
+constexpr int kMaxJobs = 80;
+struct JobTable {
+    TrackLaunch job[kMaxJobs];
+    int first[kMaxJobs + 1];
+    int njobs;
+};
+static_assert(sizeof(JobTable) < 32000, "JobTable must fit the 32 KB kernel-parameter limit");
 
 // Where a chronicle mark goes: the block's shared-memory window of the slot
 // when the word lies inside it, else the slot in global memory.
@@ -95,6 +106,8 @@ inline long long slot_words(const OnekaGrid& g) { return mask_words(g) + 4; }
 
 cudaError_t launch_track64(const TrackLaunch& L, cudaStream_t s);
 cudaError_t launch_track32(const TrackLaunch& L, cudaStream_t s);
+cudaError_t launch_track32_batch(const JobTable& T, int rows, cudaStream_t s);
+cudaError_t launch_register_batch(const JobTable& T, int rows, cudaStream_t s);
 cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid& g, int32_t* counts,
                                    cudaStream_t s);
 

@@ -68,8 +68,8 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
         if (!CONFINED) pot.add(w.w * __logf(r2));
     }
     if (CONFINED) {
-        kx = -(qx.s * m.inv_hn);
-        ky = -(qy.s * m.inv_hn);
+        kx = -((qx.s - qx.c) * m.inv_hn);
+        ky = -((qy.s - qy.c) * m.inv_hn);
         return true;
     }
     // Head from the compensated potential (model.py:341-350).  The inversion
@@ -77,20 +77,18 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
     // branch is linear), so FP32 keeps the digits the compensated sum
     // delivers.  An FP64 inversion near the aquifer top would add nothing to
     // an FP32 result and, on GB300, costs the whole warp ~1000 FP64-pipe
-    // cycles whenever one lane takes it.
+    // cycles whenever one lane takes it.  Computed without branches; a dry
+    // point (potential or head <= 0, the reference's AquiferError) is
+    // reported through the return value.
     const float phi = pot.s - pot.c;
-    if (phi <= 0.0f) return false;
     const float kh2 = m.kh2f;
-    float head;
-    if (phi < kh2)
-        head = sqrtf(2.0f * phi * m.inv_k);
-    else
-        head = (phi + kh2) * m.inv_kh;
-    if (head <= 0.0f) return false;
-    const float inv = (head > m.H) ? m.inv_hn : 1.0f / (head * m.n);
-    kx = -(qx.s * inv);
-    ky = -(qy.s * inv);
-    return true;
+    const float hu = sqrtf(fmaxf(2.0f * phi * m.inv_k, 0.0f));
+    const float hc = (phi + kh2) * m.inv_kh;
+    const float head = (phi < kh2) ? hu : hc;
+    const float inv = (head > m.H) ? m.inv_hn : __fdividef(1.0f, head * m.n);
+    kx = -((qx.s - qx.c) * inv);
+    ky = -((qy.s - qy.c) * inv);
+    return (phi > 0.0f) && (head > 0.0f);
 }
 
 // Error-free a + b = s + e (Knuth's two-sum).
@@ -268,12 +266,10 @@ struct Cold {
     }
 };
 
-// The realization's constants, re-read from shared memory at every velocity
-// evaluation (a broadcast load) rather than held in registers.
+// The realization's constants come from shared memory (block-uniform).
 template <bool CONFINED>
-__device__ __forceinline__ bool feval_c(const RealConst32& rc_, const float4* w, int nw, float x, float y,
+__device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* w, int nw, float x, float y,
                                         float& kx, float& ky) {
-    const volatile RealConst32& rc = rc_;
     Model32 m;
     m.w = w;
     m.nw = nw;
@@ -388,6 +384,7 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
     }
     float ex = c_dp_e[0] * s.k1x, ey = c_dp_e[0] * s.k1y;
     float kx = 0.0f, ky = 0.0f;
+    bool wet = true;
 #pragma unroll 1
     for (int st = 0; st < 6; ++st) {            // evaluates k2..k7
         // px[st] selected with compile-time indexes only
@@ -395,10 +392,8 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
 #pragma unroll
         for (int q = 1; q < 6; ++q)
             if (q == st) { ax = px[q]; ay = py[q]; }
-        if (!feval_c<CONFINED>(rc, w, L.nwells, s.xh + (s.xl + dt * ax), s.yh + (s.yl + dt * ay), kx, ky)) {
-            s.status = ONEKA_TRACE_DRY;
-            return false;
-        }
+        // a dry stage ends the trace after the attempt (nothing of it is kept)
+        wet &= feval_c<CONFINED>(rc, w, L.nwells, s.xh + (s.xl + dt * ax), s.yh + (s.yl + dt * ay), kx, ky);
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             px[q] += c_dp_b[st][q] * kx;
@@ -406,6 +401,10 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
         }
         ex += c_dp_e[st + 1] * kx;
         ey += c_dp_e[st + 1] * ky;
+    }
+    if (!wet) {
+        s.status = ONEKA_TRACE_DRY;
+        return false;
     }
     // kx, ky = k7 = f(xyt); the 5th-order step is dt * P_5
     const float sx = dt * px[5], sy = dt * py[5];
@@ -458,11 +457,11 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
     return s.tau_h != 0.0f;
 }
 
-template <bool CONFINED, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) track32_kernel(const TrackLaunch L, int chunks) {
+// One block: realization k of launch L (wave-local), particles of chunk blockIdx.x.
+template <bool CONFINED, int BLOCK>
+__device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks) {
     extern __shared__ float4 sm32[];
     __shared__ RealConst32 rc;
-    const int k = blockIdx.y;
     const int r = L.r0 + k;
     float4* w = sm32;
     Cold<BLOCK> cold;
@@ -531,6 +530,32 @@ __global__ void __launch_bounds__(BLOCK, MINB) track32_kernel(const TrackLaunch 
 }
 
 template <bool CONFINED, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) track32_kernel(const TrackLaunch L, int chunks) {
+    block32<CONFINED, BLOCK>(L, blockIdx.y, chunks);
+}
+
+// Many sites in one launch: row blockIdx.y belongs to job j with
+// first[j] <= row < first[j + 1]; jobs may differ in wells, paths, grid,
+// duration and aquifer type.  The table is a __grid_constant__ parameter, so
+// it is read in place (no copy) and a captured CUDA graph carries it.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) track32_batch_kernel(const __grid_constant__ JobTable T,
+                                                                     int chunks) {
+    const int row = blockIdx.y;
+    int lo = 0, hi = T.njobs - 1;
+    while (lo < hi) {                       // last job with first[j] <= row
+        const int mid = (lo + hi + 1) >> 1;
+        if (T.first[mid] <= row) lo = mid; else hi = mid - 1;
+    }
+    const TrackLaunch& J = T.job[lo];
+    const int k = row - T.first[lo];
+    if (J.opts.confined)
+        block32<true, BLOCK>(J, k, chunks);
+    else
+        block32<false, BLOCK>(J, k, chunks);
+}
+
+template <bool CONFINED, int BLOCK, int MINB>
 cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
     static int sms = 0;
     if (!sms) {
@@ -561,7 +586,7 @@ template <bool CONFINED>
 cudaError_t launch_confined(const TrackLaunch& L, cudaStream_t s) {
     // (threads per block, minimum resident blocks per SM): the variants the
     // autotuner chooses between through OnekaTrackOpts.block / .occupancy
-    const int block = L.opts.block > 0 ? L.opts.block : 128;
+    const int block = L.opts.block > 0 ? L.opts.block : 256;
     const int occ = L.opts.occupancy;
     if (block == 64) return launch_variant<CONFINED, 64, 8>(L, s);
     if (block == 256) return occ >= 3 ? launch_variant<CONFINED, 256, 3>(L, s)
@@ -572,10 +597,56 @@ cudaError_t launch_confined(const TrackLaunch& L, cudaStream_t s) {
     return launch_variant<CONFINED, 128, 4>(L, s);
 }
 
+template <int BLOCK, int MINB>
+cudaError_t launch_batch_variant(const JobTable& T, int rows, size_t smem, cudaStream_t s) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int minp = 1 << 30;
+    for (int j = 0; j < T.njobs; ++j) minp = min(minp, T.job[j].npaths);
+    const int target = 2 * sms * MINB;
+    int chunks = 1;
+    if (rows < target) {
+        chunks = (target + rows - 1) / rows;
+        const int maxc = (minp + BLOCK - 1) / BLOCK;
+        if (chunks > maxc) chunks = maxc;
+        if (chunks < 1) chunks = 1;
+    }
+    auto kern = track32_batch_kernel<BLOCK, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<dim3((unsigned)chunks, (unsigned)rows), BLOCK, smem, s>>>(T, chunks);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_track32(const TrackLaunch& L, cudaStream_t s) {
     return L.opts.confined ? launch_confined<true>(L, s) : launch_confined<false>(L, s);
+}
+
+cudaError_t launch_track32_batch(const JobTable& T, int rows, cudaStream_t s) {
+    if (T.njobs <= 0 || rows <= 0) return cudaSuccess;
+    const int block = T.job[0].opts.block > 0 ? T.job[0].opts.block : 256;
+    const int occ = T.job[0].opts.occupancy;
+    size_t smem = 0;
+    for (int j = 0; j < T.njobs; ++j) {
+        const TrackLaunch& L = T.job[j];
+        const size_t need = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)kColdFields * block +
+                            4 * (size_t)L.win_rows * L.win_words;
+        if (need > smem) smem = need;
+    }
+    if (block == 64) return launch_batch_variant<64, 8>(T, rows, smem, s);
+    if (block == 256) return occ >= 3 ? launch_batch_variant<256, 3>(T, rows, smem, s)
+                                      : launch_batch_variant<256, 2>(T, rows, smem, s);
+    if (block == 32) return launch_batch_variant<32, 16>(T, rows, smem, s);
+    if (occ >= 8) return launch_batch_variant<128, 8>(T, rows, smem, s);
+    if (occ >= 6) return launch_batch_variant<128, 6>(T, rows, smem, s);
+    return launch_batch_variant<128, 4>(T, rows, smem, s);
 }
 
 }  // namespace oneka

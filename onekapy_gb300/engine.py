@@ -372,3 +372,95 @@ def track(site: Site, real: Realizations, release, opts: TrackOptions, grid: Gri
                        C.ptr(registered), ctypes.byref(outputs.c()) if outputs else None, sptr,
                        sbytes, C.stream_ptr(stream))
     C.check(rc)
+
+
+# ---------------------------------------------------------------------------
+# autotuner: block shape, occupancy and chronicle window of the FP32 tracker
+# ---------------------------------------------------------------------------
+TUNE_CANDIDATES = [(256, 2, 32), (256, 3, 32), (128, 4, 32), (128, 6, 16), (128, 6, 32), (64, 8, 16)]
+_tuned: dict = {}
+
+
+def site_signature(site: Site, grid: Grid, opts: TrackOptions, npaths: int) -> tuple:
+    return (site.nwells, bool(opts.confined), int(opts.precision), grid.nrows, grid.ncols, int(npaths))
+
+
+def autotune(site: Site, real: Realizations, release, opts: TrackOptions, grid: Grid, *, sample=256,
+             candidates=TUNE_CANDIDATES, repeats=2, verbose=False) -> TrackOptions:
+    """Time the tracker's launch variants on a sample of the realizations and
+    return `opts` with the fastest (block, occupancy, window_kb).  Results are
+    cached per site shape for the process."""
+    key = site_signature(site, grid, opts, len(release))
+    if key in _tuned:
+        b, o, w = _tuned[key]
+        return TrackOptions(**{**opts.__dict__, "block": b, "occupancy": o, "window_kb": w})
+    n = max(1, min(sample, real.n))
+    sub = real.slice(0, n)
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=site.device)
+    scratch = scratch_buffer(grid.slot_bytes() * n, site.device)
+    best, best_t = None, float("inf")
+    for (b, o, w) in candidates:
+        trial = TrackOptions(**{**opts.__dict__, "block": b, "occupancy": o, "window_kb": w})
+        times = []
+        for _ in range(repeats + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            track(site, sub, release, trial, grid, counts=counts, scratch=scratch)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        t = min(times[1:])
+        if verbose:
+            print(f"autotune block={b} occupancy={o} window_kb={w}: {t:.3f} ms")
+        if t < best_t:
+            best, best_t = (b, o, w), t
+    _tuned[key] = best
+    return TrackOptions(**{**opts.__dict__, "block": best[0], "occupancy": best[1], "window_kb": best[2]})
+
+
+# ---------------------------------------------------------------------------
+# many sites in one launch
+# ---------------------------------------------------------------------------
+@dataclass
+class TrackJob:
+    """One site of a batched launch (oneka_track_batched)."""
+    site: Site
+    real: Realizations
+    release: torch.Tensor
+    opts: TrackOptions
+    grid: Grid
+    counts: torch.Tensor
+    registered: torch.Tensor | None = None
+
+
+def batched_scratch_bytes(jobs) -> int:
+    arr, _keep = _job_array(jobs)
+    return int(C.load().oneka_track_batched_scratch_bytes(arr, len(jobs)))
+
+
+def _job_array(jobs):
+    keep = []
+    arr = (C.OnekaTrackJob * max(1, len(jobs)))()
+    for i, j in enumerate(jobs):
+        site_c, real_c, opts_c, grid_c = j.site.c(), j.real.c(), j.opts.c(), j.grid.c()
+        keep += [site_c, real_c, opts_c, grid_c]
+        arr[i] = C.OnekaTrackJob(ctypes.pointer(site_c), ctypes.pointer(real_c), j.real.n,
+                                 int(j.release.shape[0]), C.ptr(j.release), ctypes.pointer(opts_c),
+                                 ctypes.pointer(grid_c), C.ptr(j.counts), C.ptr(j.registered), None)
+    return arr, keep
+
+
+def track_batched(jobs, scratch: torch.Tensor | None = None, stream=None) -> None:
+    """Track and chronicle every realization of every job in batched launches
+    (FP32 build; the first job's block/occupancy apply to all)."""
+    if not jobs:
+        return
+    arr, keep = _job_array(jobs)
+    if scratch is None:
+        need = int(C.load().oneka_track_batched_scratch_bytes(arr, len(jobs)))
+        scratch = scratch_buffer(min(need, 16 << 30) + 256, jobs[0].site.device)
+    base = C.ptr(scratch)
+    pad = (-base) % 256
+    C.check(C.load().oneka_track_batched(arr, len(jobs), base + pad, scratch.numel() - pad,
+                                         C.stream_ptr(stream)))
+

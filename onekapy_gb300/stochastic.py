@@ -47,6 +47,9 @@ def create_stochastic_capturezone(
     opts = E.TrackOptions(duration=duration, tol=tol, maxstep=maxstep, umbra=umbra,
                           confined=confined, precision=precision)
     release = torch.as_tensor(site.release(npaths), device=dev)
+    if precision == C.FP32 and nrealizations >= 256:
+        opts = E.autotune(site, real, release, opts, E.Grid.window(site.xt, site.yt, spacing,
+                                                                   window or 2000.0))
     pfield = ProbabilityField(spacing, spacing, site.xt, site.yt)
     if window is not None:
         grid = E.Grid.window(site.xt, site.yt, spacing, window)

@@ -56,7 +56,7 @@ def test_struct_layout_matches_header():
     """Compile a probe against the header and compare sizes/offsets with ctypes."""
     from onekapy_gb300 import _capi as C
     structs = ["OnekaDist", "OnekaSite", "OnekaRealizations", "OnekaGrid", "OnekaFrame",
-               "OnekaTrackOpts", "OnekaTrackOut"]
+               "OnekaTrackOpts", "OnekaTrackOut", "OnekaTrackJob"]
     lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){"]
     for s in structs:
         lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
