@@ -37,6 +37,9 @@ sys.path.insert(0, ROOT)
 METRIC = "realizations/s & particle-steps/s on 1 GB300 vs plain FP64; L∞ capture-prob err"
 UNIT = "realizations/s"
 SEED = 20261203
+# DRAM bytes per realization of the tracking launch on this site, from one ncu
+# capture of a 1,000-realization launch (15.62 MB; profiles/).
+TRACK32_DRAM_BYTES_PER_REALIZATION = 15.62e6 / 1000
 
 
 def args_():
@@ -161,7 +164,7 @@ def run_reference(a):
     from onekapy_gb300 import sites as S
     spec = S.config2(nreal=a.nreal, npaths=a.npaths)
     threads = host_threads()
-    sample = max(8, 2 * threads)
+    sample = 10 * max(4, threads)
     for _ in range(a.warmup):
         cpu_oracle_rate(spec, None, max(2, threads // 4), threads)
     rates, steps_rates, total = [], [], 0.0
@@ -319,7 +322,7 @@ def run_ours(a):
         cpu = None
         if world == 1 and not a.no_cpu_baseline:
             th = host_threads()
-            ns = max(4, th)
+            ns = 10 * max(4, th)      # about 1-2 s wall on 16 threads: 15-30 s of CPU work
             rate, srate, dt = cpu_oracle_rate(spec, None, ns, th)
             cpu = {"value": rate, "unit": UNIT, "cores": th, "kind": "port",
                    "sample": f"{ns} realizations x {P} paths of the workload ({dt:.1f} s wall; "
@@ -339,7 +342,10 @@ def run_ours(a):
                 "work_per_step": {"step_attempts": attempts, "accepted_steps": accepts,
                                   "chronicle_node_tests": ntests, "chronicle_word_atomics": natoms},
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak / 1e12,
-                             "unit": "TFLOP/s", "frac": achieved / (peak / 1e12), "traffic": None,
+                             "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
+                             "traffic": TRACK32_DRAM_BYTES_PER_REALIZATION * R,
+                             "traffic_source": "ncu dram__bytes_read+write of a 1000-realization launch, "
+                                               "scaled by realizations (profiles/track32_config2_1000real_full.md)",
                              "kernel": "track32_kernel (+ register_counts_kernel)",
                              "peak_source": "measured FP32 FMA loop on this GPU (oneka_fma_peak)"},
                 "e2e": {"value": e2e_n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
