@@ -270,6 +270,9 @@ def run_ours(a):
         t_step = float(t.item())
     ms_per_step = 1e3 * t_step / a.steps
     value = world * R * a.steps / t_step
+    if world > 1:   # integer sum of the ranks' count grids (after the timed region)
+        from onekapy_gb300.shard import reduce_counts
+        reduce_counts(counts, reg)
     psteps = world * accepts * a.steps / t_step
 
     line = None

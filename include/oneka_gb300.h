@@ -297,6 +297,25 @@ ONEKA_API int oneka_register_weighted(const OnekaGrid* grid, uint32_t* mask, dou
                             void* stream);
 
 /*
+ * Smoothed capture probability (oneka/visualize.py:232-233,
+ * scipy.ndimage.gaussian_filter(Z, smooth, mode='constant', cval=0)): two
+ * separable FP64 passes (columns, then rows) with zero padding.  weights:
+ * device [2*radius+1], normalized; tmp: a caller buffer like out.
+ */
+ONEKA_API int oneka_gaussian_filter(const double* in, double* out, double* tmp, int32_t nrows,
+                                    int32_t ncols, const double* weights, int32_t radius, void* stream);
+
+/*
+ * Histogram of integer visit counts (values clamped to [0, nbins - 1]),
+ * added into hist (uint64 [nbins]).  The impact curve of
+ * oneka/visualize.py:382-385 (probabilities sorted in decreasing order
+ * against cumulative area) and the decile table of oneka/oneka.py:278-288
+ * follow from its cumulative sums, since every probability is count / R.
+ */
+ONEKA_API int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nbins, uint64_t* hist,
+                                    void* stream);
+
+/*
  * Measurement helper (no reference counterpart): sustained FMA throughput of
  * this GPU in FLOP/s for FP32 (fp64 == 0) or FP64 (fp64 != 0), from a
  * register-resident FMA loop over every SM.  Synchronizes `stream`.

@@ -25,7 +25,8 @@ FP64, FP32 = 0, 1
 EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_realize",
            "oneka_track_scratch_bytes", "oneka_track", "oneka_evaluate", "oneka_rasterize",
            "oneka_register_weighted", "oneka_distancesquared", "oneka_fma_peak",
-           "oneka_track_noalloc", "oneka_track_batched", "oneka_track_batched_scratch_bytes"]
+           "oneka_track_noalloc", "oneka_track_batched", "oneka_track_batched_scratch_bytes",
+           "oneka_gaussian_filter", "oneka_count_histogram"]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
@@ -119,6 +120,10 @@ def load() -> ctypes.CDLL:
         L.oneka_track_batched_scratch_bytes.argtypes = [ctypes.POINTER(OnekaTrackJob), _I]
         L.oneka_track_batched.restype = ctypes.c_int
         L.oneka_track_batched.argtypes = [ctypes.POINTER(OnekaTrackJob), _I, _P, ctypes.c_size_t, _P]
+        L.oneka_gaussian_filter.restype = ctypes.c_int
+        L.oneka_gaussian_filter.argtypes = [_P, _P, _P, _I, _I, _P, _I, _P]
+        L.oneka_count_histogram.restype = ctypes.c_int
+        L.oneka_count_histogram.argtypes = [_P, ctypes.c_int64, _I, _P, _P]
         L.oneka_evaluate.restype = ctypes.c_int
         L.oneka_evaluate.argtypes = [ctypes.POINTER(OnekaSite), _P, _D, _D, _D,
                                      ctypes.POINTER(ctypes.c_double), _P, ctypes.c_int64, _I, _P, _P,

@@ -20,6 +20,10 @@ cudaError_t launch_rasterize(const OnekaGrid& g, const OnekaFrame& f, const doub
                              double umbra, uint32_t* mask, cudaStream_t s);
 cudaError_t launch_distancesquared(const double* abc, double* d2, long long n, cudaStream_t s);
 cudaError_t probe_fma(int fp64, double* flops_per_s, cudaStream_t s);
+cudaError_t launch_gaussian(const double* in, double* out, double* tmp, int nrows, int ncols, const double* w,
+                            int radius, cudaStream_t s);
+cudaError_t launch_histogram(const int32_t* counts, long long n, int nbins, unsigned long long* hist,
+                             cudaStream_t s);
 cudaError_t launch_evaluate(const OnekaSite& site, const double* q, double K, double n, double H,
                             const double* coef, const double* pts, long long npts, int confined,
                             double* potential, double* discharge, double* head, double* velocity,
@@ -354,6 +358,23 @@ int oneka_register_weighted(const OnekaGrid* grid, uint32_t* mask, double weight
     g_err[0] = 0;
     ONEKA_CHECK_ARG(grid_ok(grid) && mask && pgrid, "grid/mask/pgrid");
     ONEKA_CHECK_CUDA(launch_register_weighted(mask, *grid, weight, pgrid, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_gaussian_filter(const double* in, double* out, double* tmp, int32_t nrows, int32_t ncols,
+                          const double* weights, int32_t radius, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(in && out && tmp && weights && nrows > 0 && ncols > 0, "in/out/tmp/weights/shape");
+    ONEKA_CHECK_ARG(radius >= 0 && radius <= 4096, "radius");
+    ONEKA_CHECK_ARG(in != tmp && out != tmp, "tmp must not alias in or out");
+    ONEKA_CHECK_CUDA(launch_gaussian(in, out, tmp, nrows, ncols, weights, radius, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nbins, uint64_t* hist, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(counts && hist && n >= 0 && nbins > 0 && nbins <= 12000, "counts/hist/n/nbins");
+    ONEKA_CHECK_CUDA(launch_histogram(counts, n, nbins, (unsigned long long*)hist, (cudaStream_t)stream));
     return ONEKA_OK;
 }
 

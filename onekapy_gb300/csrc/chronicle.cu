@@ -178,6 +178,43 @@ __global__ void evaluate_kernel(EvalModel m, const double* __restrict__ pts, lon
     if (status) status[i] = confined ? ONEKA_TRACE_OK : st;
 }
 
+// One pass of a separable Gaussian filter with zero padding outside the grid
+// (scipy.ndimage.gaussian_filter(..., mode='constant', cval=0), used by
+// oneka/visualize.py:232-233): along rows (axis 1) when along_cols == 0, else
+// along columns (axis 0).  w: the 2*radius+1 normalized weights.
+__global__ void gauss_pass_kernel(const double* __restrict__ in, double* __restrict__ out, int nrows, int ncols,
+                                  const double* __restrict__ w, int radius, int along_cols) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nrows * ncols) return;
+    const int row = (int)(i / ncols), col = (int)(i % ncols);
+    double acc = 0.0;
+    for (int k = -radius; k <= radius; ++k) {
+        const int rr = along_cols ? row + k : row;
+        const int cc = along_cols ? col : col + k;
+        if (rr < 0 || rr >= nrows || cc < 0 || cc >= ncols) continue;
+        acc += w[k + radius] * in[(long long)rr * ncols + cc];
+    }
+    out[i] = acc;
+}
+
+// Histogram of int32 counts in [0, nbins); values outside are clamped into
+// the last bin (shared-memory privatized).
+__global__ void count_histogram_kernel(const int32_t* __restrict__ counts, long long n, int nbins,
+                                       unsigned long long* __restrict__ hist) {
+    extern __shared__ unsigned int sh[];
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0u;
+    __syncthreads();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int v = counts[i];
+        v = v < 0 ? 0 : (v >= nbins ? nbins - 1 : v);
+        atomicAdd(&sh[v], 1u);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+        if (sh[b]) atomicAdd(&hist[b], (unsigned long long)sh[b]);
+}
+
 unsigned blocks_for(long long n, int per_block) { return (unsigned)((n + per_block - 1) / per_block); }
 
 }  // namespace
@@ -187,6 +224,26 @@ cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid&
     if (nslots <= 0) return cudaSuccess;
     register_counts_kernel<<<(unsigned)nslots, 256, 0, s>>>(slots, slot_words(g), mask_words(g), g.nrows,
                                                             g.ncols, words_per_row(g.ncols), counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gaussian(const double* in, double* out, double* tmp, int nrows, int ncols, const double* w,
+                            int radius, cudaStream_t s) {
+    const long long n = (long long)nrows * ncols;
+    if (n <= 0) return cudaSuccess;
+    // axis 0 first, then axis 1, as scipy.ndimage.gaussian_filter applies its 1-D passes
+    gauss_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, tmp, nrows, ncols, w, radius, 1);
+    gauss_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(tmp, out, nrows, ncols, w, radius, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_histogram(const int32_t* counts, long long n, int nbins, unsigned long long* hist,
+                             cudaStream_t s) {
+    if (n <= 0 || nbins <= 0) return cudaSuccess;
+    long long blocks = blocks_for(n, 256);
+    if (blocks > 1216) blocks = 1216;
+    count_histogram_kernel<<<(unsigned)blocks, 256, sizeof(unsigned) * (size_t)nbins, s>>>(counts, n, nbins,
+                                                                                        hist);
     return cudaGetLastError();
 }
 

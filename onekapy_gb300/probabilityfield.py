@@ -84,6 +84,8 @@ class ProbabilityField:
     @property
     def rgrid(self) -> torch.Tensor:
         """The registration grid of the current realization as bool [nrows, ncols]."""
+        if self._mask is None and getattr(self, "_host_rgrid", None) is not None:
+            return self._host_rgrid
         return _unpack(self._mask, self.nrows, self.ncols, (self.ncols + 31) // 32)
 
     @rgrid.setter
@@ -195,6 +197,34 @@ class ProbabilityField:
         out = torch.empty(1, dtype=torch.float64, device=dev)
         C.check(C.load().oneka_distancesquared(C.ptr(q), C.ptr(out), 1, C.stream_ptr()))
         return float(out.item())
+
+    # ---------------------------------------------------------------- pickling
+    def __getstate__(self):
+        """Host arrays under the reference's attribute names (archive.py)."""
+        st = {k: v for k, v in self.__dict__.items()
+              if k not in ("_mask", "pgrid", "realizations", "counts", "_host_rgrid")}
+        if self.nrows:
+            st["pgrid"] = self.pgrid.detach().cpu().numpy()
+            st["rgrid"] = self.rgrid.cpu().numpy()
+        return st
+
+    def __setstate__(self, st):
+        st = dict(st)
+        pgrid = st.pop("pgrid", None)
+        rgrid = st.pop("rgrid", None)
+        self.__dict__.update(st)
+        self._mask = None
+        self.pgrid = None
+        self._host_rgrid = None
+        if pgrid is not None:
+            if torch.cuda.is_available():
+                dev = C.device()
+                self.pgrid = torch.as_tensor(pgrid, device=dev)
+                self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=dev)
+                self.rgrid = torch.as_tensor(rgrid, device=dev)
+            else:           # inspection without a GPU: host arrays
+                self.pgrid = torch.as_tensor(pgrid)
+                self._host_rgrid = torch.as_tensor(rgrid)
 
     # ---------------------------------------------------------------- helpers
     def probability(self) -> torch.Tensor:

@@ -81,6 +81,7 @@ def create_stochastic_capturezone(
                                   dtype=torch.uint8).to(dev)
         E.track(site, real.slice(a, b), release, opts, grid, counts=counts, registered=registered,
                 frames=fr)
+    pfield.counts = counts
     pfield.pgrid = counts.to(torch.float64)
     pfield.total_weight = float(registered.item())
     pfield.realizations = real

@@ -46,6 +46,11 @@ def import_reference(path):
     return model, capturezone, probabilityfield
 
 
+def import_reference_utilities():
+    from oneka import utilities
+    return utilities
+
+
 def make_site(rng, *, nnb, radius, nobs, obs_half, head_fn, sigma, q_target, q_nb, rw=0.25):
     wells = [(0.0, 0.0, rw, q_target)]
     for _ in range(nnb):
@@ -281,6 +286,27 @@ def main():
     np.savez_compressed(os.path.join(args.out, "expand_geometry.npz"),
                         **{f"{k}_{i}": v for i, d in enumerate(seqs) for k, v in d.items()},
                         ncases=len(seqs), **meta)
+    # ---- filter_obs: buffer removals and runs of consecutive near-duplicates.
+    U = import_reference_utilities()
+    fr = np.random.default_rng(11)
+    fcases = []
+    for k in range(4):
+        wl = [(float(x), float(y), 0.25, 500.0) for x, y in fr.uniform(-1000, 1000, size=(3 + k, 2))]
+        ob = []
+        for _ in range(30):
+            x, y = fr.uniform(-1200, 1200, size=2)
+            ob.append((float(x), float(y), float(fr.uniform(90, 110)), float(fr.choice([0.1, 0.5, 2.0]))))
+            if fr.uniform() < 0.3:      # a near-duplicate right after it
+                ob.append((float(x + fr.uniform(-0.6, 0.6)), float(y + fr.uniform(-0.6, 0.6)),
+                           float(fr.uniform(90, 110)), float(fr.choice([0.1, 0.5]))))
+        ob.append((wl[0][0] + 50.0, wl[0][1], 100.0, 1.0))   # inside the buffer of a well
+        buf = [100.0, 60.0, 0.0, 250.0][k]
+        res = U.filter_obs(ob, wl, buf)
+        fcases.append(dict(wells=np.array(wl), obs=np.array(ob), buffer=buf,
+                           retained=np.array([tuple(float(v) for v in r) for r in res])))
+    np.savez_compressed(os.path.join(args.out, "filter_obs_cases.npz"),
+                        **{f"{k}_{i}": v for i, d in enumerate(fcases) for k, v in d.items()},
+                        ncases=len(fcases), **meta)
     print("done")
 
 
