@@ -315,6 +315,62 @@ ONEKA_API int oneka_gaussian_filter(const double* in, double* out, double* tmp, 
 ONEKA_API int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nbins, uint64_t* hist,
                                     void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* Learned surrogate (no counterpart in the reference): an MLP from a
+ * realization's parameters (A..F, discharges, K, porosity) to per-cell
+ * capture logits, trained on the tracker's own per-realization masks.
+ * BF16 operands, FP32 accumulation, FP32 master weights.  All arrays are
+ * device memory; bf16 arrays are raw 16-bit words. */
+
+/*
+ * C[M][N] = A . B (+ bias[N]) (then GELU) on the tensor cores (bf16 mma,
+ * FP32 accumulate).  A is [M][lda] when a_kmajor, else [K][lda] (A^T stored
+ * row-major); B is [N][ldb] when b_kmajor, else [K][ldb].  C is FP32 when
+ * c_f32, else BF16.  Z (optional, BF16, ldc) receives the pre-activation.
+ * K % 32 == 0; lda, ldb, ldc % 8 == 0; 16-byte aligned.  splitk > 1 adds
+ * partial products into a zeroed FP32 C (no GELU, no Z).
+ */
+ONEKA_API int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B, int32_t ldb,
+                              int32_t b_kmajor, void* C, int32_t ldc, int32_t c_f32, const float* bias,
+                              int32_t gelu, void* Z, int32_t M, int32_t N, int32_t K, int32_t splitk,
+                              void* stream);
+
+/*
+ * out[n] += sum over m of sigmoid((A B^T)[m][n] + bias[n]) for k-major A [M][lda]
+ * and B [N][ldb] (BF16): the surrogate's last layer fused with the sum of its
+ * capture probabilities over realizations; the logits are never stored.
+ */
+ONEKA_API int oneka_gemm_bf16_sigmoid_colsum(const void* A, int32_t lda, const void* B, int32_t ldb,
+                                             const float* bias, float* out, int32_t M, int32_t N, int32_t K,
+                                             void* stream);
+
+/*
+ * Binary cross-entropy of logits [B][ncells] (FP32) against chronicle masks
+ * (sample b's bits at masks + b * slot_words, wpr words per grid row):
+ * loss += scale * sum(bce); dlogits (BF16, optional) = scale * (sigmoid - y).
+ */
+ONEKA_API int oneka_bce_bitmask(const float* logits, const uint32_t* masks, int64_t slot_words, int32_t wpr,
+                                int32_t ncols, int32_t B, int32_t ncells, float scale, void* dlogits,
+                                float* loss, void* stream);
+
+/* dz = dh * GELU'(z): dh FP32, z and dz BF16, n elements. */
+ONEKA_API int oneka_gelu_backward(const float* dh, const void* z, void* dz, int64_t n, void* stream);
+
+/* out[c] = sum over rows of x[r][c], x BF16 [rows][cols]. */
+ONEKA_API int oneka_colsum_bf16(const void* x, int32_t rows, int32_t cols, float* out, void* stream);
+
+/* AdamW step `step` (>= 1) on FP32 w, m, v with gradient g; writes the BF16 copy w_bf16 if given. */
+ONEKA_API int oneka_adamw(float* w, float* m, float* v, const float* g, void* w_bf16, int64_t n, float lr,
+                          float beta1, float beta2, float eps, float weight_decay, int32_t step, void* stream);
+
+/* Standardized BF16 features [n][ld] of realizations: A..F, discharges, K, porosity (nf = 8 + nwells). */
+ONEKA_API int oneka_features(const double* coef, const double* q, const double* aquifer, int32_t nwells,
+                             int32_t n, const float* mean, const float* inv_std, int32_t nf, int32_t ld,
+                             void* x, void* stream);
+
+/* out[c] += sum over rows of sigmoid(logits[r][c]) (logits FP32 [rows][cols]). */
+ONEKA_API int oneka_sigmoid_colsum(const float* logits, int32_t rows, int32_t cols, float* out, void* stream);
+
 /*
  * Measurement helper (no reference counterpart): sustained FMA throughput of
  * this GPU in FLOP/s for FP32 (fp64 == 0) or FP64 (fp64 != 0), from a

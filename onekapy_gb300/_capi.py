@@ -26,7 +26,9 @@ EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_r
            "oneka_track_scratch_bytes", "oneka_track", "oneka_evaluate", "oneka_rasterize",
            "oneka_register_weighted", "oneka_distancesquared", "oneka_fma_peak",
            "oneka_track_noalloc", "oneka_track_batched", "oneka_track_batched_scratch_bytes",
-           "oneka_gaussian_filter", "oneka_count_histogram"]
+           "oneka_gaussian_filter", "oneka_count_histogram", "oneka_gemm_bf16", "oneka_bce_bitmask",
+           "oneka_gelu_backward", "oneka_colsum_bf16", "oneka_adamw", "oneka_features",
+           "oneka_sigmoid_colsum", "oneka_gemm_bf16_sigmoid_colsum"]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
@@ -124,6 +126,23 @@ def load() -> ctypes.CDLL:
         L.oneka_gaussian_filter.argtypes = [_P, _P, _P, _I, _I, _P, _I, _P]
         L.oneka_count_histogram.restype = ctypes.c_int
         L.oneka_count_histogram.argtypes = [_P, ctypes.c_int64, _I, _P, _P]
+        L.oneka_gemm_bf16.restype = ctypes.c_int
+        L.oneka_gemm_bf16.argtypes = [_P, _I, _I, _P, _I, _I, _P, _I, _I, _P, _I, _P, _I, _I, _I, _I, _P]
+        L.oneka_bce_bitmask.restype = ctypes.c_int
+        L.oneka_bce_bitmask.argtypes = [_P, _P, ctypes.c_int64, _I, _I, _I, _I, ctypes.c_float, _P, _P, _P]
+        L.oneka_gelu_backward.restype = ctypes.c_int
+        L.oneka_gelu_backward.argtypes = [_P, _P, _P, ctypes.c_int64, _P]
+        L.oneka_colsum_bf16.restype = ctypes.c_int
+        L.oneka_colsum_bf16.argtypes = [_P, _I, _I, _P, _P]
+        L.oneka_adamw.restype = ctypes.c_int
+        L.oneka_adamw.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_float, ctypes.c_float, _I, _P]
+        L.oneka_features.restype = ctypes.c_int
+        L.oneka_features.argtypes = [_P, _P, _P, _I, _I, _P, _P, _I, _I, _P, _P]
+        L.oneka_sigmoid_colsum.restype = ctypes.c_int
+        L.oneka_sigmoid_colsum.argtypes = [_P, _I, _I, _P, _P]
+        L.oneka_gemm_bf16_sigmoid_colsum.restype = ctypes.c_int
+        L.oneka_gemm_bf16_sigmoid_colsum.argtypes = [_P, _I, _P, _I, _P, _P, _I, _I, _I, _P]
         L.oneka_evaluate.restype = ctypes.c_int
         L.oneka_evaluate.argtypes = [ctypes.POINTER(OnekaSite), _P, _D, _D, _D,
                                      ctypes.POINTER(ctypes.c_double), _P, ctypes.c_int64, _I, _P, _P,

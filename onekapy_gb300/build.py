@@ -35,6 +35,7 @@ UNITS = {
     "track32.cu": ["--fmad=true", "--use_fast_math"],
     "probe.cu": ["--fmad=true"],
     "noalloc.cu": ["--fmad=false"],
+    "mlp.cu": ["--fmad=true"],
 }
 
 

@@ -24,6 +24,18 @@ cudaError_t launch_gaussian(const double* in, double* out, double* tmp, int nrow
                             int radius, cudaStream_t s);
 cudaError_t launch_histogram(const int32_t* counts, long long n, int nbins, unsigned long long* hist,
                              cudaStream_t s);
+cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B, int ldb, int b_kmajor, void* C,
+                             int ldc, int c_f32, const float* bias, int gelu, void* Z, int M, int N, int K,
+                             int splitk, float* sigsum, cudaStream_t s);
+cudaError_t launch_bce_bitmask(const float* logits, const uint32_t* masks, long long slot_words, int wpr, int ncols,
+                               int B, int ncells, float scale, void* dlogits, float* loss, cudaStream_t s);
+cudaError_t launch_gelu_backward(const float* dh, const void* z, void* dz, long long n, cudaStream_t s);
+cudaError_t launch_colsum(const void* x, int rows, int cols, float* out, cudaStream_t s);
+cudaError_t launch_adamw(float* w, float* m, float* v, const float* g, void* wb, long long n, float lr, float b1,
+                         float b2, float eps, float wd, int step, cudaStream_t s);
+cudaError_t launch_features(const double* coef, const double* q, const double* aquifer, int nwells, int n,
+                            const float* mean, const float* inv_std, int nf, int ld, void* x, cudaStream_t s);
+cudaError_t launch_sigmoid_colsum(const float* logits, int rows, int cols, float* out, cudaStream_t s);
 cudaError_t launch_evaluate(const OnekaSite& site, const double* q, double K, double n, double H,
                             const double* coef, const double* pts, long long npts, int confined,
                             double* potential, double* discharge, double* head, double* velocity,
@@ -375,6 +387,83 @@ int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nbins, uint6
     g_err[0] = 0;
     ONEKA_CHECK_ARG(counts && hist && n >= 0 && nbins > 0 && nbins <= 12000, "counts/hist/n/nbins");
     ONEKA_CHECK_CUDA(launch_histogram(counts, n, nbins, (unsigned long long*)hist, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B, int32_t ldb, int32_t b_kmajor,
+                    void* C, int32_t ldc, int32_t c_f32, const float* bias, int32_t gelu, void* Z, int32_t M,
+                    int32_t N, int32_t K, int32_t splitk, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(A && B && C && M > 0 && N > 0 && K > 0, "A/B/C/M/N/K");
+    ONEKA_CHECK_ARG(K % 32 == 0, "K must be a multiple of 32");
+    ONEKA_CHECK_ARG(lda % 8 == 0 && ldb % 8 == 0 && ldc % 8 == 0, "leading dimensions must be multiples of 8");
+    ONEKA_CHECK_ARG(al16(A) && al16(B) && al16(C) && (!Z || al16(Z)), "16-byte aligned matrices");
+    ONEKA_CHECK_ARG(lda >= (a_kmajor ? K : M) && ldb >= (b_kmajor ? K : N) && ldc >= N, "leading dimensions");
+    ONEKA_CHECK_ARG(splitk <= 1 || (c_f32 && !gelu && !Z), "split-K needs an FP32 output without GELU");
+    ONEKA_CHECK_CUDA(launch_gemm_bf16(A, lda, a_kmajor, B, ldb, b_kmajor, C, ldc, c_f32, bias, gelu, Z, M, N, K,
+                                      splitk, nullptr, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_gemm_bf16_sigmoid_colsum(const void* A, int32_t lda, const void* B, int32_t ldb, const float* bias,
+                                   float* out, int32_t M, int32_t N, int32_t K, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(A && B && out && M > 0 && N > 0 && K > 0, "A/B/out/M/N/K");
+    ONEKA_CHECK_ARG(K % 32 == 0, "K must be a multiple of 32");
+    ONEKA_CHECK_ARG(lda % 8 == 0 && ldb % 8 == 0 && lda >= K && ldb >= K, "leading dimensions");
+    ONEKA_CHECK_ARG(al16(A) && al16(B), "16-byte aligned matrices");
+    ONEKA_CHECK_CUDA(launch_gemm_bf16(A, lda, 1, B, ldb, 1, nullptr, N, 1, bias, 0, nullptr, M, N, K, 1, out,
+                                      (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_bce_bitmask(const float* logits, const uint32_t* masks, int64_t slot_words, int32_t wpr, int32_t ncols,
+                      int32_t B, int32_t ncells, float scale, void* dlogits, float* loss, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(logits && masks && B > 0 && ncells > 0 && ncols > 0 && wpr * 32 >= ncols, "bce arguments");
+    ONEKA_CHECK_CUDA(launch_bce_bitmask(logits, masks, slot_words, wpr, ncols, B, ncells, scale, dlogits, loss,
+                                        (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_gelu_backward(const float* dh, const void* z, void* dz, int64_t n, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(dh && z && dz && n >= 0, "gelu_backward arguments");
+    ONEKA_CHECK_CUDA(launch_gelu_backward(dh, z, dz, n, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_colsum_bf16(const void* x, int32_t rows, int32_t cols, float* out, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(x && out && rows > 0 && cols > 0, "colsum arguments");
+    ONEKA_CHECK_CUDA(launch_colsum(x, rows, cols, out, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_adamw(float* w, float* m, float* v, const float* g, void* w_bf16, int64_t n, float lr, float beta1,
+                float beta2, float eps, float weight_decay, int32_t step, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(w && m && v && g && n >= 0 && step >= 1, "adamw arguments");
+    ONEKA_CHECK_CUDA(launch_adamw(w, m, v, g, w_bf16, n, lr, beta1, beta2, eps, weight_decay, step,
+                                  (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_features(const double* coef, const double* q, const double* aquifer, int32_t nwells, int32_t n,
+                   const float* mean, const float* inv_std, int32_t nf, int32_t ld, void* x, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(coef && q && aquifer && mean && inv_std && x && n >= 0, "features arguments");
+    ONEKA_CHECK_ARG(nf == 6 + nwells + 2 && ld >= nf, "nf = 6 + nwells + 2 and ld >= nf");
+    ONEKA_CHECK_CUDA(launch_features(coef, q, aquifer, nwells, n, mean, inv_std, nf, ld, x, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_sigmoid_colsum(const float* logits, int32_t rows, int32_t cols, float* out, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(logits && out && rows > 0 && cols > 0, "sigmoid_colsum arguments");
+    ONEKA_CHECK_CUDA(launch_sigmoid_colsum(logits, rows, cols, out, (cudaStream_t)stream));
     return ONEKA_OK;
 }
 

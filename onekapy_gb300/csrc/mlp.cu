@@ -1,0 +1,393 @@
+// mlp.cu -- kernels of the learned surrogate: a BF16 tensor-core GEMM with
+// fused bias/GELU epilogues, the BCE loss against chronicle bitmasks, GELU
+// backward, bias gradients and the AdamW update (FP32 master weights).
+//
+// The surrogate maps a realization's parameter vector (A..F, discharges, K,
+// porosity) to per-cell capture logits; its training labels are the
+// per-realization bitmasks the tracker chronicles (oneka_track mark-only
+// mode).  It has no counterpart in the reference.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "oneka_internal.cuh"
+
+namespace oneka {
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, THREADS = 256;
+constexpr int KPAD = BK + 8;      // k-major tiles: rows of 40 bf16 (80 B)
+constexpr int MPAD = BM + 8;      // m/n-major tiles: rows of 136 bf16 (272 B)
+
+struct GemmArgs {
+    const __nv_bfloat16* A;   // k-major: [M][lda]; m-major: [K][lda]
+    const __nv_bfloat16* B;   // k-major: [N][ldb]; n-major: [K][ldb]
+    void* C;                  // [M][ldc], bf16 or f32
+    __nv_bfloat16* Z;         // pre-activation copy (bf16, ldc), or null
+    const float* bias;        // [N] or null
+    float* sigsum;            // non-null: out[n] += sum over rows of sigmoid(C[m][n]); C not written
+    int M, N, K, lda, ldb, ldc;
+    int c_f32, gelu, kper;    // kper: K range of one split
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+    const int n = valid ? 16 : 0;   // 0: zero-fill, nothing read
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(n));
+}
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                 "{%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+// C = A * B (+ bias, GELU) with FP32 accumulation.  Block 128 x 128, 8 warps
+// of 64 x 32, three cp.async stages of BK = 32.  Rows/columns beyond M or N
+// are zero-filled on load and skipped on store; K must be a multiple of 32
+// and the leading dimensions multiples of 8 (16-byte rows).  gridDim.z
+// splits K: each split adds its partial product into a zeroed FP32 C.
+template <bool A_KMAJOR, bool B_KMAJOR>
+__global__ void __launch_bounds__(THREADS) gemm_bf16_kernel(const GemmArgs g) {
+    extern __shared__ __align__(16) unsigned char gsm[];
+    constexpr int A_ELEMS = A_KMAJOR ? BM * KPAD : BK * MPAD;
+    constexpr int B_ELEMS = B_KMAJOR ? BN * KPAD : BK * MPAD;
+    __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(gsm);
+    __nv_bfloat16* Bs = As + STAGES * A_ELEMS;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp >> 2, wn = warp & 3;             // 2 x 4 warps
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int kbeg = blockIdx.z * g.kper;
+    const int kend = min(g.K, kbeg + g.kper);
+    const int ktiles = (kend - kbeg) / BK;
+
+    auto load_stage = [&](int stage, int kt) {
+        const int k0 = kbeg + kt * BK;
+        __nv_bfloat16* as = As + stage * A_ELEMS;
+        __nv_bfloat16* bs = Bs + stage * B_ELEMS;
+#pragma unroll
+        for (int c = tid; c < 512; c += THREADS) {
+            if (A_KMAJOR) {          // 128 rows x 4 chunks
+                const int row = c >> 2, ch = c & 3;
+                const bool ok = m0 + row < g.M;
+                cp_async16(as + row * KPAD + ch * 8, g.A + (long long)(ok ? m0 + row : 0) * g.lda + k0 + ch * 8, ok);
+            } else {                 // 32 k-rows x 16 chunks
+                const int row = c >> 4, ch = c & 15;
+                const bool ok = m0 + ch * 8 < g.M;
+                cp_async16(as + row * MPAD + ch * 8, g.A + (long long)(k0 + row) * g.lda + (ok ? m0 + ch * 8 : 0), ok);
+            }
+            if (B_KMAJOR) {
+                const int row = c >> 2, ch = c & 3;
+                const bool ok = n0 + row < g.N;
+                cp_async16(bs + row * KPAD + ch * 8, g.B + (long long)(ok ? n0 + row : 0) * g.ldb + k0 + ch * 8, ok);
+            } else {
+                const int row = c >> 4, ch = c & 15;
+                const bool ok = n0 + ch * 8 < g.N;
+                cp_async16(bs + row * MPAD + ch * 8, g.B + (long long)(k0 + row) * g.ldb + (ok ? n0 + ch * 8 : 0), ok);
+            }
+        }
+    };
+
+    float acc[4][4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < ktiles) load_stage(s, s);
+        cp_commit();
+    }
+    for (int kt = 0; kt < ktiles; ++kt) {
+        cp_wait<STAGES - 2>();
+        __syncthreads();
+        const int nxt = kt + STAGES - 1;
+        if (nxt < ktiles) load_stage(nxt % STAGES, nxt);
+        cp_commit();
+        const __nv_bfloat16* as = As + (kt % STAGES) * A_ELEMS;
+        const __nv_bfloat16* bs = Bs + (kt % STAGES) * B_ELEMS;
+#pragma unroll
+        for (int kk = 0; kk < BK; kk += 16) {
+            uint32_t af[4][4], bfr[4][2];
+            const int q = lane >> 3, r8 = lane & 7;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int mb = wm * 64 + i * 16;
+                if (A_KMAJOR)
+                    ldsm_x4(af[i][0], af[i][1], af[i][2], af[i][3],
+                            as + (mb + (lane & 15)) * KPAD + kk + (lane >> 4) * 8);
+                else
+                    ldsm_x4_t(af[i][0], af[i][1], af[i][2], af[i][3],
+                              as + (kk + r8 + (q >> 1) * 8) * MPAD + mb + (q & 1) * 8);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j += 2) {
+                const int nb = wn * 32 + j * 8;
+                if (B_KMAJOR)
+                    ldsm_x4(bfr[j][0], bfr[j][1], bfr[j + 1][0], bfr[j + 1][1],
+                            bs + (nb + r8 + (q >> 1) * 8) * KPAD + kk + (q & 1) * 8);
+                else
+                    ldsm_x4_t(bfr[j][0], bfr[j][1], bfr[j + 1][0], bfr[j + 1][1],
+                              bs + (kk + r8 + (q & 1) * 8) * MPAD + nb + (q >> 1) * 8);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j][0], bfr[j][1]);
+        }
+    }
+    cp_wait<0>();
+
+    if (g.sigsum) {
+        // Column sums of sigmoid(logits) over this warp's 64 rows: each lane
+        // holds 8 rows of 8 columns; lanes with equal (lane & 3) share
+        // columns, so a butterfly over lane bits 2..4 finishes the sum.
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int n = n0 + wn * 32 + j * 8 + (lane & 3) * 2 + e;
+                const float bn = (n < g.N && g.bias) ? g.bias[n] : 0.0f;
+                float s = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int m = m0 + wm * 64 + i * 16 + (lane >> 2) + h * 8;
+                        if (m < g.M) s += 1.0f / (1.0f + __expf(-(acc[i][j][h * 2 + e] + bn)));
+                    }
+                s += __shfl_xor_sync(0xffffffffu, s, 4);
+                s += __shfl_xor_sync(0xffffffffu, s, 8);
+                s += __shfl_xor_sync(0xffffffffu, s, 16);
+                if (lane < 4 && n < g.N) atomicAdd(g.sigsum + n, s);
+            }
+        }
+        return;
+    }
+    const bool split = gridDim.z > 1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int m = m0 + wm * 64 + i * 16 + (lane >> 2) + h * 8;
+                if (m >= g.M) continue;
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int n = n0 + wn * 32 + j * 8 + (lane & 3) * 2 + e;
+                    if (n >= g.N) continue;
+                    float v = acc[i][j][h * 2 + e];
+                    if (g.bias && blockIdx.z == 0) v += g.bias[n];
+                    const long long off = (long long)m * g.ldc + n;
+                    if (split) {
+                        atomicAdd(reinterpret_cast<float*>(g.C) + off, v);
+                        continue;
+                    }
+                    if (g.Z) g.Z[off] = __float2bfloat16(v);
+                    if (g.gelu) v = gelu_f(v);
+                    if (g.c_f32)
+                        reinterpret_cast<float*>(g.C)[off] = v;
+                    else
+                        reinterpret_cast<__nv_bfloat16*>(g.C)[off] = __float2bfloat16(v);
+                }
+            }
+        }
+    }
+}
+
+// Mean binary cross-entropy of logits z against the bits of a chronicle
+// mask (cell i*ncols + j <-> bit j%32 of word i*wpr + j/32 of the sample's
+// slot), and its gradient (sigmoid(z) - y) * scale as BF16.
+__global__ void bce_bitmask_kernel(const float* __restrict__ logits, const uint32_t* __restrict__ masks,
+                                   long long slot_words, int wpr, int ncols, int B, int ncells, float scale,
+                                   __nv_bfloat16* __restrict__ dlogits, float* __restrict__ loss) {
+    const long long n = (long long)B * ncells;
+    float part = 0.0f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(i / ncells), c = (int)(i % ncells);
+        const int row = c / ncols, col = c % ncols;
+        const uint32_t w = masks[(long long)b * slot_words + (long long)row * wpr + (col >> 5)];
+        const float y = (float)((w >> (col & 31)) & 1u);
+        const float z = logits[i];
+        part += fmaxf(z, 0.0f) - z * y + log1pf(expf(-fabsf(z)));
+        const float p = 1.0f / (1.0f + expf(-z));
+        if (dlogits) dlogits[i] = __float2bfloat16((p - y) * scale);
+    }
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, part * scale);
+}
+
+// dz = dh * gelu'(z), dh in FP32, z (pre-activation) and dz in BF16.
+__global__ void gelu_backward_kernel(const float* __restrict__ dh, const __nv_bfloat16* __restrict__ z,
+                                     __nv_bfloat16* __restrict__ dz, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        dz[i] = __float2bfloat16(dh[i] * gelu_grad(__bfloat162float(z[i])));
+}
+
+// out[c] = sum_r x[r][c] (bias gradients), x in BF16, one thread per column.
+__global__ void colsum_kernel(const __nv_bfloat16* __restrict__ x, int rows, int cols, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float s = 0.0f;
+    for (int r = 0; r < rows; ++r) s += __bfloat162float(x[(long long)r * cols + c]);
+    out[c] = s;
+}
+
+// AdamW with bias correction (decoupled weight decay), FP32 master weights,
+// and the BF16 copy the GEMMs read.
+__global__ void adamw_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                             const float* __restrict__ g, __nv_bfloat16* __restrict__ wb, long long n, float lr,
+                             float b1, float b2, float eps, float wd, float c1, float c2) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float upd = (mi / c1) / (sqrtf(vi / c2) + eps);
+        const float wi = w[i] - lr * (upd + wd * w[i]);
+        w[i] = wi;
+        if (wb) wb[i] = __float2bfloat16(wi);
+    }
+}
+
+// Standardized features of realizations [first, first + n) as BF16 rows of
+// ld columns (zero beyond nf): A..F, discharges, then K and porosity.
+__global__ void features_kernel(const double* __restrict__ coef, const double* __restrict__ q,
+                                const double* __restrict__ aquifer, int nwells, int n, const float* __restrict__ mean,
+                                const float* __restrict__ inv_std, int nf, int ld, __nv_bfloat16* __restrict__ x) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n * ld) return;
+    const int r = (int)(i / ld), f = (int)(i % ld);
+    float v = 0.0f;
+    if (f < nf) {
+        double raw;
+        if (f < 6) raw = coef[6LL * r + f];
+        else if (f < 6 + nwells) raw = q[(long long)r * nwells + (f - 6)];
+        else raw = aquifer[3LL * r + (f - 6 - nwells)];
+        v = ((float)raw - mean[f]) * inv_std[f];
+    }
+    x[i] = __float2bfloat16(v);
+}
+
+// out[c] += sum_r sigmoid(logits[r][c]): the surrogate's expected visits per cell.
+__global__ void sigmoid_colsum_kernel(const float* __restrict__ logits, int rows, int cols, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float s = 0.0f;
+    for (int r = 0; r < rows; ++r) s += 1.0f / (1.0f + expf(-logits[(long long)r * cols + c]));
+    out[c] += s;
+}
+
+unsigned grid_for(long long n, int per) {
+    long long b = (n + per - 1) / per;
+    return (unsigned)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+}
+
+}  // namespace
+
+cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B, int ldb, int b_kmajor, void* C,
+                             int ldc, int c_f32, const float* bias, int gelu, void* Z, int M, int N, int K,
+                             int splitk, float* sigsum, cudaStream_t s) {
+    GemmArgs g;
+    g.A = (const __nv_bfloat16*)A;
+    g.B = (const __nv_bfloat16*)B;
+    g.C = C;
+    g.Z = (__nv_bfloat16*)Z;
+    g.bias = bias;
+    g.sigsum = sigsum;
+    g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.ldc = ldc;
+    g.c_f32 = c_f32;
+    g.gelu = gelu;
+    if (splitk < 1) splitk = 1;
+    int ktiles = K / BK;
+    if (splitk > ktiles) splitk = ktiles > 0 ? ktiles : 1;
+    g.kper = ((ktiles + splitk - 1) / splitk) * BK;
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, splitk);
+    const size_t smA = (size_t)STAGES * (a_kmajor ? BM * KPAD : BK * MPAD) * 2;
+    const size_t smB = (size_t)STAGES * (b_kmajor ? BN * KPAD : BK * MPAD) * 2;
+    const int smem = (int)(smA + smB);
+#define ONEKA_GEMM_CASE(AK, BKM)                                                                          \
+    {                                                                                                     \
+        cudaError_t e = cudaFuncSetAttribute(gemm_bf16_kernel<AK, BKM>,                                   \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);          \
+        if (e != cudaSuccess) return e;                                                                   \
+        gemm_bf16_kernel<AK, BKM><<<grid, THREADS, smem, s>>>(g);                                         \
+    }
+    if (a_kmajor && b_kmajor) ONEKA_GEMM_CASE(true, true)
+    else if (a_kmajor) ONEKA_GEMM_CASE(true, false)
+    else if (b_kmajor) ONEKA_GEMM_CASE(false, true)
+    else ONEKA_GEMM_CASE(false, false)
+#undef ONEKA_GEMM_CASE
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bce_bitmask(const float* logits, const uint32_t* masks, long long slot_words, int wpr, int ncols,
+                               int B, int ncells, float scale, void* dlogits, float* loss, cudaStream_t s) {
+    bce_bitmask_kernel<<<grid_for((long long)B * ncells, 256), 256, 0, s>>>(
+        logits, masks, slot_words, wpr, ncols, B, ncells, scale, (__nv_bfloat16*)dlogits, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gelu_backward(const float* dh, const void* z, void* dz, long long n, cudaStream_t s) {
+    gelu_backward_kernel<<<grid_for(n, 256), 256, 0, s>>>(dh, (const __nv_bfloat16*)z, (__nv_bfloat16*)dz, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_colsum(const void* x, int rows, int cols, float* out, cudaStream_t s) {
+    colsum_kernel<<<(cols + 255) / 256, 256, 0, s>>>((const __nv_bfloat16*)x, rows, cols, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adamw(float* w, float* m, float* v, const float* g, void* wb, long long n, float lr, float b1,
+                         float b2, float eps, float wd, int step, cudaStream_t s) {
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    adamw_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, m, v, g, (__nv_bfloat16*)wb, n, lr, b1, b2, eps, wd, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sigmoid_colsum(const float* logits, int rows, int cols, float* out, cudaStream_t s) {
+    sigmoid_colsum_kernel<<<(cols + 255) / 256, 256, 0, s>>>(logits, rows, cols, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_features(const double* coef, const double* q, const double* aquifer, int nwells, int n,
+                            const float* mean, const float* inv_std, int nf, int ld, void* x, cudaStream_t s) {
+    const long long tot = (long long)n * ld;
+    if (tot <= 0) return cudaSuccess;
+    features_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(coef, q, aquifer, nwells, n, mean, inv_std, nf,
+                                                                  ld, (__nv_bfloat16*)x);
+    return cudaGetLastError();
+}
+
+}  // namespace oneka

@@ -15,6 +15,9 @@ definitions:
             256^2-1024^2 grids at 5-20 m).
   config 4  unconfined, water table 0.5-3 m above the base near the target,
             target Q ~ U(1000, 3000), 30 neighbour wells, 5,000 x 2,048, 25 years.
+  config 5  the surrogate's fixed site: 1 + 30 wells, mixed aquifer (top 30 m),
+            20 m grid of 256 x 256 nodes; 39 varying parameters per
+            realization (A..F, 31 discharges, K, porosity).
 
 Heads of the confined/mixed sites come from a seeded quadratic head surface
 (A, B ~ 1e-7, C ~ 1e-8, D, E ~ 1e-3) plus N(0, sigma) noise; the unconfined
@@ -137,3 +140,14 @@ def config3(seed: int = 1003, nsites: int = 64):
                               (0.2, 0.3), (20.0, 30.0), True, years * DAY_PER_YEAR, npaths, nreal,
                               spacing, 2 * spacing, 0.5 * (side - 1) * spacing))
     return sites
+
+
+def config5(seed: int = 1005, nreal: int = 200000, npaths: int = 1000) -> SiteSpec:
+    """The surrogate's fixed 31-well site (config-2 style, 20 m grid of 256 x 256)."""
+    rng = np.random.default_rng(seed)
+    wells = [(0.0, 0.0, 0.25, (400.0, 600.0))] + _neighbours(rng, 30, 5000.0, (100.0, 500.0))
+    obs = _quadratic_heads(rng, 60, 3000.0, 30.0, 0.1)
+    return SiteSpec("config5-surrogate-31wells", wells, obs, 0.0, Lognormal(np.log(10.0), 0.3),
+                    (0.2, 0.3), 30.0, False, 20 * DAY_PER_YEAR, npaths, nreal, 20.0, 20.0,
+                    0.5 * 255 * 20.0)
+

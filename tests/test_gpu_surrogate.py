@@ -1,0 +1,156 @@
+"""GPU: the surrogate's kernels (GEMM layouts, gradients, AdamW) against
+FP32/FP64 references, and the trained surrogate against the tracker."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from onekapy_gb300 import _capi as C  # noqa: E402
+from onekapy_gb300 import engine as E  # noqa: E402
+from onekapy_gb300 import sites as S  # noqa: E402
+from onekapy_gb300 import surrogate as SG  # noqa: E402
+
+
+@pytest.mark.parametrize("a_kmajor,b_kmajor", [(True, True), (True, False), (False, True), (False, False)])
+@pytest.mark.parametrize("M,N,K,splitk", [(256, 384, 96, 1), (200, 72, 64, 1), (128, 512, 1024, 8)])
+def test_gemm_layouts_match_fp32(a_kmajor, b_kmajor, M, N, K, splitk):
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(M + N + K)
+    A = torch.randn((M, K), generator=g).to(dev)
+    B = torch.randn((K, N), generator=g).to(dev)
+    bias = torch.randn(N, generator=g).to(dev) if splitk == 1 else None
+    Ab = (A if a_kmajor else A.T.contiguous()).to(torch.bfloat16).contiguous()
+    Bb = (B.T.contiguous() if b_kmajor else B).to(torch.bfloat16).contiguous()
+    Cf = torch.zeros((M, N), dtype=torch.float32, device=dev)
+    SG.gemm(Ab, a_kmajor, Bb, b_kmajor, Cf, M, N, K, bias=bias, splitk=splitk)
+    ref = (Ab.float() if a_kmajor else Ab.float().T) @ (Bb.float().T if b_kmajor else Bb.float())
+    if bias is not None:
+        ref = ref + bias
+    assert torch.allclose(Cf, ref, rtol=1e-3, atol=1e-3 * math.sqrt(K))
+
+
+def test_gemm_gelu_epilogue():
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(3)
+    A = torch.randn((256, 64), generator=g).to(dev).to(torch.bfloat16)
+    W = torch.randn((128, 64), generator=g).to(dev).to(torch.bfloat16)
+    b = torch.randn(128, generator=g).to(dev)
+    H = torch.empty((256, 128), dtype=torch.bfloat16, device=dev)
+    Z = torch.empty_like(H)
+    SG.gemm(A, True, W, True, H, 256, 128, 64, bias=b, gelu=True, Z=Z)
+    z = A.float() @ W.float().T + b
+    assert torch.allclose(Z.float(), z, rtol=2e-2, atol=2e-2)
+    assert torch.allclose(H.float(), torch.nn.functional.gelu(z), rtol=2e-2, atol=2e-2)
+
+
+def test_mlp_gradients_match_cpu_oracle():
+    import mlp_oracle
+    dev = C.device()
+    dims = [64, 96, 96, 64, 512]
+    model = SG.MLP(dims, dev, seed=1)
+    Bn = 64
+    g = torch.Generator(device="cpu").manual_seed(9)
+    X = (torch.randn((Bn, 64), generator=g) * 0.8).to(dev).to(torch.bfloat16)
+    # labels: a 16 x 32 grid per sample in the chronicle's bitmask layout
+    bits = (torch.rand((Bn, 16, 32), generator=g) < 0.3)
+    words = (bits.to(torch.int64) << torch.arange(32)).sum(-1)            # [B][16] one word per row
+    masks = torch.where(words >= 2**31, words - 2**32, words).to(torch.int32).reshape(Bn, 16).to(dev)
+    model.forward(X)
+    loss = model.loss_and_grad(masks, 16, 1, 32)
+    model.backward()
+    torch.cuda.synchronize()
+    W = [L.wb.float().cpu().double().numpy() for L in model.layers]
+    bvec = [L.b.cpu().double().numpy() for L in model.layers]
+    lo, dW, db = mlp_oracle.forward_backward(X.float().cpu().double().numpy(), W, bvec,
+                                             bits.reshape(Bn, 512).double().numpy())
+    assert abs(float(loss.item()) - lo) < 1e-3 * max(1.0, abs(lo))
+    for i, L in enumerate(model.layers):
+        gw = L.gw.cpu().double().numpy()
+        gb = L.gb.cpu().double().numpy()
+        assert np.linalg.norm(gw - dW[i]) <= 0.03 * np.linalg.norm(dW[i]) + 1e-12, i
+        assert np.linalg.norm(gb - db[i]) <= 0.03 * np.linalg.norm(db[i]) + 1e-12, i
+
+
+def test_adamw_matches_restatement():
+    import mlp_oracle
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(4)
+    w = torch.randn(1000, generator=g)
+    m = torch.randn(1000, generator=g) * 0.1
+    v = torch.rand(1000, generator=g) * 0.1
+    grad = torch.randn(1000, generator=g)
+    wd, md, vd, gd = (t.to(dev).contiguous() for t in (w, m, v, grad))
+    wb = torch.empty(1000, dtype=torch.bfloat16, device=dev)
+    C.check(C.load().oneka_adamw(C.ptr(wd), C.ptr(md), C.ptr(vd), C.ptr(gd), C.ptr(wb), 1000, 1e-3, 0.9, 0.999,
+                                 1e-8, 1e-2, 7, C.stream_ptr()))
+    w2, m2, v2 = mlp_oracle.adamw(w.double().numpy(), m.double().numpy(), v.double().numpy(),
+                                  grad.double().numpy(), 1e-3, 0.9, 0.999, 1e-8, 1e-2, 7)
+    assert np.allclose(wd.cpu().numpy(), w2, rtol=1e-5, atol=1e-6)
+    assert np.allclose(md.cpu().numpy(), m2, rtol=1e-5, atol=1e-6)
+    assert torch.equal(wb, wd.to(torch.bfloat16))
+
+
+def test_fused_sigmoid_colsum_matches_fp32():
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(11)
+    for M, N, K in [(300, 520, 64), (2048, 4096, 256)]:
+        H = torch.randn((M, K), generator=g).to(dev).to(torch.bfloat16)
+        W = (torch.randn((N, K), generator=g) * 0.2).to(dev).to(torch.bfloat16)
+        b = torch.randn(N, generator=g).to(dev)
+        out = torch.full((N,), 0.5, dtype=torch.float32, device=dev)
+        C.check(C.load().oneka_gemm_bf16_sigmoid_colsum(C.ptr(H), K, C.ptr(W), K, C.ptr(b), C.ptr(out), M, N, K,
+                                                        C.stream_ptr()))
+        ref = 0.5 + torch.sigmoid(H.float() @ W.float().T + b).sum(0)
+        assert torch.allclose(out, ref, rtol=1e-4, atol=1e-3 * math.sqrt(M))
+
+
+def test_trained_surrogate_screens_faster_within_tolerance():
+    """Train on tracker-chronicled masks of the 31-well site (1000 paths, 20
+    years, a 128 x 128 grid at 20 m, 8 k realizations), then screen 8 k
+    fresh realizations with 5 % judges: the judges accept the surrogate, the
+    screened field agrees with tracking every realization, and screening
+    costs less than tracking everything."""
+    dev = C.device()
+    spec = S.config5(npaths=1000)
+    site = E.Site(spec.wells, spec.observations, spec.base, c_dist=spec.c_dist, p_dist=spec.p_dist,
+                  t_dist=spec.t_dist, device=dev)
+    nr = nc = 128
+    grid = E.Grid(site.xt - 1270.0, site.yt - 1270.0, 20.0, 20.0, nr, nc)
+    release = torch.as_tensor(site.release(spec.npaths), device=dev)
+    opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=False, precision=C.FP32)
+    train_real = E.realize(site, 8192, seed=77)
+    masks, slot_words = SG.chronicle_masks(site, train_real, release, opts, grid)
+    feats = SG.Features(train_real, site.nwells)
+    X = feats(train_real)
+    model = SG.MLP([64, 256, 256, 256, nr * nc], dev, seed=3, out_bias=math.log(0.05 / 0.95))
+    losses = SG.train(model, X, masks, slot_words, grid.words_per_row, nc, epochs=4, batch=256, lr=2e-3,
+                      lr_final=2e-4)
+    assert losses[-1] < 0.5 * losses[0], losses
+    fresh = E.realize(site, 8192, seed=78)
+    SG.screen(model, feats, site, fresh.slice(0, 1024), release, opts, grid, judge_fraction=0.05,
+              tolerance=1.0)                                   # warm-up
+    res = SG.screen(model, feats, site, fresh, release, opts, grid, judge_fraction=0.05, tolerance=0.1)
+    assert res.accepted, (res.judge_linf, res.judge_l1)
+    counts = torch.zeros((nr, nc), dtype=torch.int32, device=dev)
+    E.track(site, fresh.slice(0, 1024), release, opts, grid, counts=counts)   # warm-up
+    counts.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    E.track(site, fresh, release, opts, grid, counts=counts)
+    e1.record()
+    torch.cuda.synchronize()
+    t_track = e0.elapsed_time(e1) / 1e3
+    full = counts.double() / fresh.n
+    err = (res.field - full).abs()
+    print(f"surrogate screen: loss {losses[0]:.4f} -> {losses[-1]:.4f}; judges {res.n_judges} "
+          f"L-inf {res.judge_linf:.4f} L1 {res.judge_l1:.2e}; field vs all-tracked L-inf "
+          f"{float(err.max()):.4f} L1 {float(err.mean()):.2e}; screen {res.seconds * 1e3:.1f} ms "
+          f"(judges {res.seconds_judges * 1e3:.1f}, surrogate {res.seconds_surrogate * 1e3:.1f}) vs "
+          f"track-all {t_track * 1e3:.1f} ms")
+    assert float(err.max()) < 0.1
+    assert res.seconds < t_track, (res.seconds, t_track)
