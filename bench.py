@@ -16,6 +16,22 @@ kernel against the measured FP32 FMA peak, and the oracle CPU port timed on
 this host's cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Other workloads (one JSON line each; the default line above is the headline):
+
+    --workload config3   64 uneven sites (2-200 wells, 1k-20k realizations,
+                         360/1024/4096 paths, 5-50 years, 256^2-1024^2 grids) in
+                         one batched launch sequence replayed as a CUDA graph,
+                         against one oneka_track call per site.
+    --workload config4   unconfined stress site (31 wells, water table 0.5-3 m
+                         above the base near the target, 5,000 x 2,048, 25 years):
+                         the FP32 build timed, and its per-cell capture-probability
+                         errors and endpoint drift against the all-FP64 run.
+    --workload config5   the learned surrogate on the fixed 31-well site: 200,000
+                         tracker-chronicled training pairs, MLP 39 -> 3 x 512 GELU ->
+                         256 x 256 logits trained with the project's kernels, then
+                         100,000 fresh realizations screened with 5 % judges,
+                         against tracking all of them.
 """
 from __future__ import annotations
 
@@ -50,8 +66,13 @@ def args_():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nreal", type=int, default=10000)
     ap.add_argument("--npaths", type=int, default=1000)
-    ap.add_argument("--fp64-sample", type=int, default=200)
+    ap.add_argument("--fp64-sample", type=int, default=None,
+                    help="realizations of the FP64 comparison (config2: 200; config4: all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"])
+    ap.add_argument("--fraction", type=float, default=1.0,
+                    help="config3/config5: fraction of the realization counts run")
+    ap.add_argument("--epochs", type=int, default=6, help="config5: training epochs")
     return ap.parse_args()
 
 
@@ -278,7 +299,7 @@ def run_ours(a):
     line = None
     if rank == 0:
         # plain FP64 GPU tracker and the FP32 build on the same sample of realizations
-        n64 = min(a.fp64_sample, R)
+        n64 = min(a.fp64_sample or 200, R)
         step(o64, min(8, n64))
         torch.cuda.synchronize()
         e64 = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -374,9 +395,337 @@ def ctypes_peak(C, fp64):
     return v.value
 
 
+# ---------------------------------------------------------------------------
+# other workloads
+# ---------------------------------------------------------------------------
+def _setup():
+    import torch
+    from onekapy_gb300 import _capi as C
+    from onekapy_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    return C.device()
+
+
+def _site(spec, dev):
+    from onekapy_gb300 import engine as E
+    return E.Site(spec.wells, spec.observations, spec.base, c_dist=spec.c_dist, p_dist=spec.p_dist,
+                  t_dist=spec.t_dist, device=dev)
+
+
+def _opts(spec, precision):
+    from onekapy_gb300 import engine as E
+    return E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=spec.confined, precision=precision)
+
+
+def _line(a, value, unit, metric, config, dtype="f32", **extra):
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": "synthetic", "config": config} | extra
+
+
+def _timed(fn, a, stream, flush):
+    """W untimed calls, then K calls timed with events, L2 flushed between."""
+    import torch
+    for _ in range(a.warmup):
+        fn()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    ms = []
+    for k in range(a.steps):
+        flush.fill_(k & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms, sampler.stop()
+
+
+def run_config3(a):
+    """64 uneven sites: realize + batched tracking of every site, captured
+    once as a CUDA graph and replayed per step; one oneka_track call per site
+    (the unbatched form) timed beside it; both must give the same counts."""
+    import torch
+    from onekapy_gb300 import _capi as C
+    from onekapy_gb300 import engine as E
+    from onekapy_gb300 import sites as S
+    dev = _setup()
+    specs = S.config3()
+    jobs = []
+    for k, spec in enumerate(specs):
+        site = _site(spec, dev)
+        n = max(1, int(round(spec.nreal * a.fraction)))
+        real = E.Realizations.empty(n, site.nwells, dev, with_fit=False)
+        E.realize(site, n, seed=SEED + k, out=real)
+        grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+        jobs.append(E.TrackJob(site, real, torch.as_tensor(site.release(spec.npaths), device=dev),
+                               _opts(spec, C.FP32), grid,
+                               torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev),
+                               torch.zeros(1, dtype=torch.int64, device=dev)))
+    tot_real = sum(j.real.n for j in jobs)
+    tot_part = sum(j.real.n * j.release.shape[0] for j in jobs)
+    # launch shape: autotuned on the site with the most particle work (setup, untimed)
+    big = max(jobs, key=lambda j: j.real.n * j.release.shape[0] * j.opts.duration)
+    tuned = E.autotune(big.site, big.real, big.release, big.opts, big.grid, sample=min(big.real.n, 1024))
+    for j in jobs:
+        j.opts = E.TrackOptions(**{**j.opts.__dict__, "block": tuned.block, "occupancy": tuned.occupancy,
+                                   "window_kb": tuned.window_kb})
+    need = E.batched_scratch_bytes(jobs)
+    scratch = torch.zeros(min(need, 32 << 30) + 256, dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def body():
+        for k, j in enumerate(jobs):
+            j.counts.zero_()
+            j.registered.zero_()
+            E.realize(j.site, j.real.n, seed=SEED + k, out=j.real)
+        E.track_batched(jobs, scratch=scratch)
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        body()                                     # warm every kernel before capture
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        body()
+    stream = torch.cuda.current_stream()
+    ms, clocks = _timed(graph.replay, a, stream, flush)
+    batched = [j.counts.clone() for j in jobs]
+    # work counters (untimed pass)
+    for j in jobs:
+        j.outputs = E.TrackOutputs(counters=torch.zeros(4, dtype=torch.int64, device=dev))
+    body()
+    torch.cuda.synchronize()
+    accepts = sum(int(j.outputs.counters[1].item()) for j in jobs)
+    attempts = sum(int(j.outputs.counters[0].item()) for j in jobs)
+    for j in jobs:
+        j.outputs = None
+    # one call per site (realize + oneka_track), same realizations
+    def per_site():
+        for k, j in enumerate(jobs):
+            j.counts.zero_()
+            j.registered.zero_()
+            E.realize(j.site, j.real.n, seed=SEED + k, out=j.real)
+            E.track(j.site, j.real, j.release, j.opts, j.grid, counts=j.counts, registered=j.registered,
+                    scratch=scratch)
+    a1 = argparse.Namespace(**{**a.__dict__, "warmup": 1, "steps": 1})
+    ms_site, _ = _timed(per_site, a1, stream, flush)
+    same = all(torch.equal(b, j.counts) for b, j in zip(batched, jobs))
+    t = float(np.mean(ms)) / 1e3
+    cfg = {"workload": f"config3-64-uneven-sites: {tot_real} realizations, {tot_part} particles "
+                       f"(fraction {a.fraction} of each site's realizations)",
+           "sites": len(jobs), "realizations": tot_real, "particles": tot_part,
+           "l2": "512 MB buffer written between timed steps", "graph": "realize + batched track, one replay"}
+    line = _line(a, tot_real / t, UNIT, METRIC + " (64 uneven sites, batched)", cfg,
+                 ms_per_step=1e3 * t, particle_steps_per_s=accepts / t, particles_per_s=tot_part / t,
+                 work_per_step={"step_attempts": attempts, "accepted_steps": accepts},
+                 per_site_calls={"ms_per_step": ms_site[0], "realizations_per_s": tot_real / (ms_site[0] / 1e3),
+                                 "batched_speedup": ms_site[0] / (1e3 * t)},
+                 counts_equal_batched_vs_per_site=bool(same),
+                 tracker_launch={"block": tuned.block, "occupancy": tuned.occupancy,
+                                 "window_kb": tuned.window_kb},
+                 clocks=clocks)
+    print(json.dumps(line))
+
+
+def run_config4(a):
+    """Unconfined stress site: FP32 build timed; per-cell capture-probability
+    error and endpoint drift of the FP32 build against the all-FP64 run of the
+    same realizations."""
+    import torch
+    from onekapy_gb300 import _capi as C
+    from onekapy_gb300 import engine as E
+    from onekapy_gb300 import sites as S
+    dev = _setup()
+    spec = S.config4()
+    site = _site(spec, dev)
+    R, P = spec.nreal, spec.npaths
+    grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+    release = torch.as_tensor(site.release(P), device=dev)
+    real = E.Realizations.empty(R, site.nwells, dev, with_fit=False)
+    E.realize(site, R, seed=SEED, out=real)
+    o32 = E.autotune(site, real, release, _opts(spec, C.FP32), grid, sample=min(R, 1024))
+    o64 = _opts(spec, C.FP64)
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+    scratch = torch.zeros(grid.slot_bytes() * R, dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step32():
+        counts.zero_()
+        E.realize(site, R, seed=SEED, out=real)
+        E.track(site, real, release, o32, grid, counts=counts, scratch=scratch)
+
+    ms, clocks = _timed(step32, a, stream, flush)
+    n64 = min(a.fp64_sample or R, R)
+    sub = real.slice(0, n64)
+    res = {}
+    for name, o in (("fp32", o32), ("fp64", o64)):
+        c = torch.zeros_like(counts)
+        out = E.TrackOutputs.alloc(n64, P, dev, endpoint=True, stats=True, counters=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        E.track(site, sub, release, o, grid, counts=c, scratch=scratch, outputs=out)
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = (c, out, e0.elapsed_time(e1) / 1e3)
+    c32, out32, t32 = res["fp32"]
+    c64, out64, t64 = res["fp64"]
+    diff = (c32 - c64).abs().double() / n64
+    visited = (c64 > 0) | (c32 > 0)
+    ok = (out32.status == C.TRACE_OK) & (out64.status == C.TRACE_OK)
+    drift = ((out32.endpoint - out64.endpoint).norm(dim=-1) / spec.spacing)[ok]
+    q = torch.quantile(drift.float(), torch.tensor([0.5, 0.99, 0.999], device=dev)).tolist() if drift.numel() else [0, 0, 0]
+    status_agree = float((out32.status == out64.status).double().mean().item())
+    t = float(np.mean(ms)) / 1e3
+    steps = int(out32.counters[1].item()) * R / n64
+    cfg = {"workload": "config4-unconfined-31wells: 5000 realizations x 2048 paths, 25 y, 5 m grid 8x8 km",
+           "nreal": R, "npaths": P, "fp64_realizations": n64, "l2": "512 MB buffer written between timed steps"}
+    line = _line(a, R / t, UNIT, METRIC + " (unconfined stress)", cfg, ms_per_step=1e3 * t,
+                 particle_steps_per_s=steps / t,
+                 fp64_gpu={"realizations_per_s": n64 / t64, "speedup_fp32_over_fp64": (R / t) / (n64 / t64)},
+                 fp32_vs_fp64_per_cell={"linf_capture_probability": float(diff.max().item()),
+                                        "mean_abs_over_visited_cells": float(diff[visited].mean().item())
+                                        if bool(visited.any()) else 0.0,
+                                        "cells_above_0.01": int((diff > 0.01).sum().item()),
+                                        "visited_cells": int(visited.sum().item()),
+                                        "mismatched_visited_fraction":
+                                            float(((c32 > 0) != (c64 > 0)).sum().item()) / max(1, int(visited.sum().item()))},
+                 endpoint_drift_cells={"p50": q[0], "p99": q[1], "p999": q[2],
+                                       "max": float(drift.max().item()) if drift.numel() else 0.0,
+                                       "within_1e-3_cell": float((drift <= 1e-3).double().mean().item())
+                                       if drift.numel() else 1.0,
+                                       "particles_compared": int(drift.numel())},
+                 status_agreement=status_agree,
+                 tracker_launch={"block": o32.block, "occupancy": o32.occupancy, "window_kb": o32.window_kb},
+                 clocks=clocks)
+    print(json.dumps(line))
+
+
+def run_config5(a):
+    """The learned surrogate: train on tracker-chronicled masks, then screen
+    fresh realizations with judges; compare with tracking all of them."""
+    import math
+    import torch
+    from onekapy_gb300 import _capi as C
+    from onekapy_gb300 import engine as E
+    from onekapy_gb300 import sites as S
+    from onekapy_gb300 import surrogate as SG
+    dev = _setup()
+    spec = S.config5()
+    site = _site(spec, dev)
+    ntrain = int(round(200000 * a.fraction))
+    nscreen = int(round(100000 * a.fraction))
+    side = 256
+    grid = E.Grid(site.xt - 0.5 * (side - 1) * spec.spacing, site.yt - 0.5 * (side - 1) * spec.spacing,
+                  spec.spacing, spec.spacing, side, side)
+    release = torch.as_tensor(site.release(spec.npaths), device=dev)
+    opts = E.autotune(site, E.realize(site, 1024, seed=1), release, _opts(spec, C.FP32), grid, sample=1024)
+    stream = torch.cuda.current_stream()
+    # training pairs: realizations and their chronicle masks
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    train_real = E.realize(site, ntrain, seed=SEED)
+    masks, slot_words = SG.chronicle_masks(site, train_real, release, opts, grid)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    feats = SG.Features(train_real, site.nwells)
+    X = feats(train_real)
+    visit_rate = float(torch.count_nonzero(masks[:, :grid.nrows * grid.words_per_row]).item())
+    model = SG.MLP([64, 512, 512, 512, side * side], dev, seed=5, out_bias=math.log(0.02 / 0.98))
+    t0 = time.perf_counter()
+    losses = SG.train(model, X, masks, slot_words, grid.words_per_row, side, epochs=a.epochs, batch=512,
+                      lr=1.5e-3, lr_final=1e-4)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    nsteps = a.epochs * (ntrain // 512)
+    flops_step = 3 * 2 * 512 * sum(i * o for i, o in zip(model.dims[:-1], model.dims[1:]))
+    del masks
+    # GEMM roofline: the last layer's forward GEMM of a 512-realization batch
+    xb = X[:512]
+    h = model._hidden(xb)
+    L = model.layers[-1]
+    logits = torch.empty((512, side * side), dtype=torch.float32, device=dev)
+    gm = lambda: SG.gemm(h, True, L.wb, True, logits, 512, side * side, 512, bias=L.b)
+    for _ in range(3):
+        gm()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        gm()
+    e1.record()
+    torch.cuda.synchronize()
+    t_gemm = e0.elapsed_time(e1) / 1e3 / 20
+    gemm_tf = 2 * 512 * side * side * 512 / t_gemm / 1e12
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
+    # screening of fresh realizations, end to end (draw + judges + surrogate)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    fresh = E.Realizations.empty(nscreen, site.nwells, dev, with_fit=False)
+    results = []
+
+    def screen_once():
+        E.realize(site, nscreen, seed=SEED + 1, out=fresh)
+        results.append(SG.screen(model, feats, site, fresh, release, opts, grid, judge_fraction=0.05,
+                                 tolerance=0.05))
+
+    ms, clocks = _timed(screen_once, a, stream, flush)
+    res = results[-1]
+    # tracking every fresh realization (the method without the surrogate)
+    counts = torch.zeros((side, side), dtype=torch.int32, device=dev)
+
+    def track_all():
+        counts.zero_()
+        E.realize(site, nscreen, seed=SEED + 1, out=fresh)
+        E.track(site, fresh, release, opts, grid, counts=counts)
+
+    a1 = argparse.Namespace(**{**a.__dict__, "warmup": 1, "steps": 2})
+    ms_all, _ = _timed(track_all, a1, stream, flush)
+    full = counts.double() / nscreen
+    err = (res.field - full).abs()
+    t = float(np.mean(ms)) / 1e3
+    t_all = float(np.mean(ms_all)) / 1e3
+    cfg = {"workload": f"config5-surrogate-31wells: train {ntrain} pairs, screen {nscreen} realizations "
+                       f"(5 % judges), 1000 paths, 20 y, 256x256 grid at 20 m",
+           "mlp": "39 (padded 64) -> 512 -> 512 -> 512 GELU -> 65536 logits, BF16 with FP32 master weights",
+           "l2": "512 MB buffer written between timed steps"}
+    line = _line(a, nscreen / t, UNIT, METRIC + " (surrogate-screened)", cfg, dtype="bf16",
+                 ms_per_step=1e3 * t,
+                 track_all={"ms_per_step": 1e3 * t_all, "realizations_per_s": nscreen / t_all},
+                 speedup_over_track_all=t_all / t,
+                 judges={"n": res.n_judges, "linf": res.judge_linf, "mean_abs": res.judge_l1,
+                         "tolerance": 0.05, "accepted": res.accepted},
+                 field_vs_track_all={"linf": float(err.max().item()), "mean_abs": float(err.mean().item())},
+                 screen_breakdown_ms={"judges_tracked": 1e3 * res.seconds_judges,
+                                      "surrogate": 1e3 * res.seconds_surrogate},
+                 training={"pairs": ntrain, "chronicle_seconds": t_data, "epochs": a.epochs, "steps": nsteps,
+                           "seconds": t_train, "achieved_tflops": flops_step * nsteps / t_train / 1e12,
+                           "loss_first": losses[0], "loss_last": losses[-1],
+                           "visited_word_fraction": visit_rate / (ntrain * grid.nrows * grid.words_per_row)},
+                 roofline={"bound": "tensor", "kernel": "gemm_bf16_kernel (last layer, 512 x 65536 x 512)",
+                           "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                           "frac": gemm_tf / peaks["bf16_tflops"], "traffic": None,
+                           "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst) of measured"},
+                 clocks=clocks)
+    print(json.dumps(line))
+
+
 if __name__ == "__main__":
     a = args_()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "config3":
+        run_config3(a)
+    elif a.workload == "config4":
+        run_config4(a)
+    elif a.workload == "config5":
+        run_config5(a)
     else:
         run_ours(a)

@@ -3,21 +3,25 @@
 // Same algorithm as the FP64 parity build (oneka/capturezone.py:198-253 step
 // control, oneka/model.py:269-427 velocity, oneka/probabilityfield.py:264-339
 // chronicle) with the bulk arithmetic in FP32:
-//   * coordinates are relative to the target well; the particle position is
-//     a float pair (hi + lo) updated with an error-free two-sum, so the
-//     position keeps ~48 bits over hundreds of steps;
+//   * coordinates are relative to the target well, where every trace starts;
+//     the particle position is a float pair (hi + lo) updated with an
+//     error-free two-sum, so the position keeps ~48 bits over hundreds of
+//     steps;
 //   * well terms are summed with Kahan compensation (discharge and potential);
 //   * the head is inverted from the compensated potential in FP32 (the
 //     inversion is well conditioned; see feval32);
-//   * elapsed time is kept in FP64.
+//   * the time left is a float pair counting down to zero, so no FP64
+//     instruction runs in the step loop (GB300's FP64 pipe is ~1/64 of FP32,
+//     and float<->int conversions use FP32 magic-constant arithmetic).
 //
 // Work layout: one block per realization (or per chunk of its particles when
 // the realizations alone cannot fill the GPU).  Each lane takes the next
 // particle from a shared counter as soon as its trace ends, so a block's
 // lanes stay busy until its last particles, and no lane waits for the
-// slowest trace of a fixed group.  The Dormand-Prince stage vectors live in
-// shared memory ([stage][x|y][lane]), so the velocity evaluation is inlined
-// once and the per-thread state stays small.
+// slowest trace of a fixed group.  The Dormand-Prince stages are folded into
+// register running sums of the tableau rows (one velocity evaluation inlined
+// in a loop over the six stages); the cold per-particle state (bounding box,
+// counters, frame, vertex count) sits in shared-memory columns, one per lane.
 #include <math.h>
 
 #include "oneka_internal.cuh"

@@ -431,6 +431,7 @@ class TrackJob:
     grid: Grid
     counts: torch.Tensor
     registered: torch.Tensor | None = None
+    outputs: TrackOutputs | None = None
 
 
 def batched_scratch_bytes(jobs) -> int:
@@ -443,10 +444,12 @@ def _job_array(jobs):
     arr = (C.OnekaTrackJob * max(1, len(jobs)))()
     for i, j in enumerate(jobs):
         site_c, real_c, opts_c, grid_c = j.site.c(), j.real.c(), j.opts.c(), j.grid.c()
-        keep += [site_c, real_c, opts_c, grid_c]
+        out_c = j.outputs.c() if j.outputs is not None else None
+        keep += [site_c, real_c, opts_c, grid_c, out_c]
         arr[i] = C.OnekaTrackJob(ctypes.pointer(site_c), ctypes.pointer(real_c), j.real.n,
                                  int(j.release.shape[0]), C.ptr(j.release), ctypes.pointer(opts_c),
-                                 ctypes.pointer(grid_c), C.ptr(j.counts), C.ptr(j.registered), None)
+                                 ctypes.pointer(grid_c), C.ptr(j.counts), C.ptr(j.registered),
+                                 ctypes.pointer(out_c) if out_c is not None else None)
     return arr, keep
 
 
