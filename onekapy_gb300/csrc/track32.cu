@@ -127,82 +127,110 @@ __device__ __forceinline__ bool clip_int(int lo, int hi, int n, int& ilo, int& i
     return ilo < ihi;
 }
 
-// OR the nodes gj in [glo, ghi] of grid row gi into the chronicle.
+// OR the nodes gj in [glo, ghi] of grid row gi into the chronicle (the
+// row's window test is made once, not per word).
 __device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int ghi, long long& natom) {
+    const int ri = gi - ch.r0;
+    const bool row_in = ch.win && (unsigned)ri < (unsigned)ch.nr;
     int w = glo >> 5;
     const int wl = ghi >> 5;
+    natom += wl - w + 1;
     uint32_t m = 0xffffffffu << (glo & 31);
     for (; w <= wl; ++w) {
         if (w == wl) m &= 0xffffffffu >> (31 - (ghi & 31));
-        ch.orw(gi, w, m);
-        ++natom;
+        const int wi = w - ch.w0;
+        if (row_in && (unsigned)wi < (unsigned)ch.nw)
+            atomicOr(ch.win + ri * ch.nw + wi, m);
+        else
+            atomicOr(ch.slot + (long long)gi * ch.wpr + w, m);
         m = 0xffffffffu;
     }
 }
 
+// Grid constants of the FP32 chronicle, converted once per block.
+struct Raster32 {
+    float dx, dy, inv_dx, inv_dy;
+    float U, U2;         // umbra and umbra^2 in units of dx
+    float ryy;           // row spacing in units of dx (dy / dx)
+    float umbra;
+};
+
 // Chronicle one segment in FP32: for every grid row the nodes within umbra
-// of the segment form one interval, the row's intersection with the capsule
-// (the two end disks and the band between them); the interval's nodes are
-// set as whole bit ranges.  Nodes strictly closer than umbra are marked, as
-// in ProbabilityField.insert (probabilityfield.py:296-310); FP32 rounding can
-// move a node lying within ~1e-6 m of the boundary across it.
+// of the segment form one open interval (LO, HI), the row's intersection
+// with the capsule (the two end disks and the band between them); its nodes
+// floor(LO) + 1 .. ceil(HI) - 1 are set as whole bit ranges.  Nodes strictly
+// closer than umbra are marked, as in ProbabilityField.insert
+// (probabilityfield.py:296-310); FP32 rounding can move a node lying within
+// ~1e-6 m of the boundary across it.
+//
+// Geometry is in units of dx with x measured from the frame's first column,
+// so LO and HI are node indices; every per-row quantity is one multiply-add
+// of the row's offset from the segment's start (the band's limits are
+// linear in it, with their order fixed per segment).
 __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols, int coff, int roff,
-                                         int fncols, int fnrows, float fx0, float fy0, float dx, float dy,
-                                         float umbra,
+                                         int fncols, int fnrows, float fx0, float fy0, const Raster32& g,
                                          float ax, float ay, float bx, float by, long long& ntest,
                                          long long& natom, int& rlo, int& rhi) {
     const float bax = bx - ax;
     const float bay = by - ay;
-    const float length2 = bax * bax + bay * bay;
-    if (!(length2 > 0.0f)) return;           // the reference's 0/0 marks nothing
-    const float inv_dx = 1.0f / dx, inv_dy = 1.0f / dy;
+    if (!(bax * bax + bay * bay > 0.0f)) return;    // the reference's 0/0 marks nothing
     int left, right, bottom, top;
-    if (!clip_int(floor_small((fminf(ax, bx) - umbra - fx0) * inv_dx),
-                  floor_small((fmaxf(ax, bx) + umbra - fx0) * inv_dx) + 1, fncols, left, right))
+    if (!clip_int(floor_small((fminf(ax, bx) - g.umbra - fx0) * g.inv_dx),
+                  floor_small((fmaxf(ax, bx) + g.umbra - fx0) * g.inv_dx) + 1, fncols, left, right))
         return;
-    if (!clip_int(floor_small((fminf(ay, by) - umbra - fy0) * inv_dy),
-                  floor_small((fmaxf(ay, by) + umbra - fy0) * inv_dy) + 1, fnrows, bottom, top))
+    if (!clip_int(floor_small((fminf(ay, by) - g.umbra - fy0) * g.inv_dy),
+                  floor_small((fmaxf(ay, by) + g.umbra - fy0) * g.inv_dy) + 1, fnrows, bottom, top))
         return;
     ntest += (long long)(right - left) * (top - bottom);
-    const float u2 = umbra * umbra;
-    const float uL = umbra * sqrtf(length2);
-    const float inv_bay = (bay != 0.0f) ? 1.0f / bay : 0.0f;
-    const float inv_bax = (bax != 0.0f) ? 1.0f / bax : 0.0f;
-    for (int i = bottom; i < top; ++i) {
+    // segment in units of dx: X from column 0 of the frame, Y from row 0
+    const float aX = (ax - fx0) * g.inv_dx, aY = (ay - fy0) * g.inv_dx;
+    const float bX = (bx - fx0) * g.inv_dx, bY = (by - fy0) * g.inv_dx;
+    const float BAX = bX - aX, BAY = bY - aY;
+    const float L2 = BAX * BAX + BAY * BAY;
+    const float UL = g.U * sqrtf(L2);
+    // band |BAY s - BAX t| < U L (t = row offset from a, s = X - aX):
+    //   s in (k t - |e|, k t + |e|), k = BAX / BAY, e = U L / BAY
+    // projection 0 <= BAX s + BAY t <= L^2:
+    //   s in [-m t + min(0, f), -m t + max(0, f)], m = BAY / BAX, f = L^2 / BAX
+    const bool bay_nz = BAY != 0.0f, bax_nz = BAX != 0.0f;
+    const float iby = bay_nz ? 1.0f / BAY : 0.0f, ibx = bax_nz ? 1.0f / BAX : 0.0f;
+    const float k = BAX * iby, ae = fabsf(UL * iby);
+    const float m = BAY * ibx, f = L2 * ibx;
+    const float flo = fminf(0.0f, f), fhi = fmaxf(0.0f, f);
+    const float xlo = i2f_small(left) - 1.0f, xhi = i2f_small(right);
+    float t = i2f_small(bottom) * g.ryy - aY;       // row offset from a (units of dx)
+    for (int i = bottom; i < top; ++i, t += g.ryy) {
         const int gi = i + roff;
         if (gi < 0 || gi >= gnrows) continue;
-        const float cy = fy0 + i2f_small(i) * dy;
-        const float cay = cy - ay, cby = cy - by;
-        float lo = INFINITY, hi = -INFINITY;
-        const float ha = u2 - cay * cay;
-        if (ha > 0.0f) { const float h = sqrtf(ha); lo = ax - h; hi = ax + h; }
-        const float hb = u2 - cby * cby;
-        if (hb > 0.0f) { const float h = sqrtf(hb); lo = fminf(lo, bx - h); hi = fmaxf(hi, bx + h); }
-        // band: s = x - ax with |bay s - bax cay| < u L and 0 <= bax s + bay cay <= L^2
-        float slo = -INFINITY, shi = INFINITY;
-        const float bc = bax * cay;
-        if (bay != 0.0f) {
-            const float c1 = (bc - uL) * inv_bay, c2 = (bc + uL) * inv_bay;
-            slo = fminf(c1, c2);
-            shi = fmaxf(c1, c2);
-        } else if (!(fabsf(bc) < uL)) {
-            slo = INFINITY;
+        float LO = INFINITY, HI = -INFINITY;
+        const float ha = g.U2 - t * t;
+        if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
+        const float tb = t - BAY;
+        const float hb = g.U2 - tb * tb;
+        if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bX - h); HI = fmaxf(HI, bX + h); }
+        float slo, shi;
+        if (bay_nz) {
+            const float kt = k * t;
+            slo = kt - ae;
+            shi = kt + ae;
+        } else {
+            const bool in = fabsf(t) < g.U;
+            slo = in ? -INFINITY : INFINITY;
+            shi = in ? INFINITY : -INFINITY;
         }
-        const float yc = bay * cay;
-        if (bax != 0.0f) {
-            const float d1 = -yc * inv_bax, d2 = (length2 - yc) * inv_bax;
-            slo = fmaxf(slo, fminf(d1, d2));
-            shi = fminf(shi, fmaxf(d1, d2));
-        } else if (!(yc >= 0.0f && yc <= length2)) {
-            slo = INFINITY;
+        if (bax_nz) {
+            const float mt = -m * t;
+            slo = fmaxf(slo, mt + flo);
+            shi = fminf(shi, mt + fhi);
+        } else {
+            const float yc = BAY * t;
+            if (!(yc >= 0.0f && yc <= L2)) slo = INFINITY;
         }
-        if (slo < shi) { lo = fminf(lo, ax + slo); hi = fmaxf(hi, ax + shi); }
-        if (!(lo < hi)) continue;
-        int jlo = max(ceil_small((lo - fx0) * inv_dx), left);
-        int jhi = min(floor_small((hi - fx0) * inv_dx), right - 1);
-        // strictly inside: drop an end node that sits on the boundary
-        if (jlo <= jhi && fx0 + i2f_small(jlo) * dx <= lo) ++jlo;
-        if (jlo <= jhi && fx0 + i2f_small(jhi) * dx >= hi) --jhi;
+        if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
+        if (!(LO < HI)) continue;
+        // nodes strictly inside (LO, HI), within the segment's columns [left, right)
+        const int jlo = floor_small(fmaxf(LO, xlo)) + 1;
+        const int jhi = ceil_small(fminf(HI, xhi)) - 1;
         int glo = jlo + coff, ghi = jhi + coff;
         glo = glo < 0 ? 0 : glo;
         ghi = ghi >= gncols ? gncols - 1 : ghi;
@@ -234,7 +262,8 @@ __constant__ float c_dp_e[7] = {(float)DP::e1, 0.0f, (float)DP::e3, (float)DP::e
 
 struct RealConst32 {
     float c0, c1, c2, c3, c4, c5, K, n, H, inv_hn, ox, oy, kh2f, inv_k, inv_kh;
-    float tol, maxstep, dx, dy, umbra;   // options, converted once
+    float tol, maxstep;  // options, converted once
+    Raster32 g;          // grid constants of the chronicle
     int skip;
     int next;            // next particle of this block's chunk
 };
@@ -439,7 +468,7 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
             long long ntest = (unsigned)c.i(kNtest), natom = (unsigned)c.i(kNatom);
             int rlo = c.i(kRlo), rhi = c.i(kRhi);
             insert32(ch, L.grid.nrows, L.grid.ncols, c.i(kCoff), c.i(kRoff), c.i(kNcols), c.i(kNrows),
-                     c.f(kFx0), c.f(kFy0), rc.dx, rc.dy, rc.umbra, ax, ay,
+                     c.f(kFx0), c.f(kFy0), rc.g, ax, ay,
                      bxn, byn, ntest, natom, rlo, rhi);
             c.i(kNtest) = (int)ntest;
             c.i(kNatom) = (int)natom;
@@ -488,9 +517,14 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
         rc.inv_kh = (float)(1.0 / (Kd * Hd));
         rc.tol = (float)L.opts.tol;
         rc.maxstep = (float)L.opts.maxstep;
-        rc.dx = (float)L.grid.dx;
-        rc.dy = (float)L.grid.dy;
-        rc.umbra = (float)L.opts.umbra;
+        rc.g.dx = (float)L.grid.dx;
+        rc.g.dy = (float)L.grid.dy;
+        rc.g.inv_dx = (float)(1.0 / L.grid.dx);
+        rc.g.inv_dy = (float)(1.0 / L.grid.dy);
+        rc.g.U = (float)(L.opts.umbra / L.grid.dx);
+        rc.g.U2 = rc.g.U * rc.g.U;
+        rc.g.ryy = (float)(L.grid.dy / L.grid.dx);
+        rc.g.umbra = (float)L.opts.umbra;
         rc.ox = (float)(L.xo - L.xt);
         rc.oy = (float)(L.yo - L.yt);
         rc.skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
