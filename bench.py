@@ -709,7 +709,10 @@ def run_config5(a):
                            "seconds": t_train, "achieved_tflops": flops_step * nsteps / t_train / 1e12,
                            "loss_first": losses[0], "loss_last": losses[-1],
                            "visited_word_fraction": visit_rate / (ntrain * grid.nrows * grid.words_per_row)},
-                 roofline={"bound": "tensor", "kernel": "gemm_bf16_kernel (last layer, 512 x 65536 x 512)",
+                 roofline={"bound": "tensor",
+                           "kernel": ("gemm_tc_kernel (tcgen05, TMEM accumulators, TMA; last layer 512 x 65536 x 512, "
+                                      "FP32 logits)" if SG.gemm_path(True, True, 512) else
+                                      "gemm_bf16_kernel (mma.sync; last layer 512 x 65536 x 512)"),
                            "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                            "frac": gemm_tf / peaks["bf16_tflops"], "traffic": None,
                            "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst) of measured"},

@@ -323,17 +323,33 @@ ONEKA_API int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nb
  * device memory; bf16 arrays are raw 16-bit words. */
 
 /*
- * C[M][N] = A . B (+ bias[N]) (then GELU) on the tensor cores (bf16 mma,
- * FP32 accumulate).  A is [M][lda] when a_kmajor, else [K][lda] (A^T stored
+ * C[M][N] = A . B (+ bias[N]) (then GELU) on the tensor cores, FP32
+ * accumulate.  A is [M][lda] when a_kmajor, else [K][lda] (A^T stored
  * row-major); B is [N][ldb] when b_kmajor, else [K][ldb].  C is FP32 when
  * c_f32, else BF16.  Z (optional, BF16, ldc) receives the pre-activation.
- * K % 32 == 0; lda, ldb, ldc % 8 == 0; 16-byte aligned.  splitk > 1 adds
+ * K % 32 == 0; lda, ldb, ldc % 8 == 0; matrices and bias 16-byte aligned.  splitk > 1 adds
  * partial products into a zeroed FP32 C (no GELU, no Z).
+ *
+ * K-major A and B with K % 64 == 0 and no split-K run on the tcgen05 kernel
+ * (TMA-staged operands, accumulator in tensor memory; FP32 C, or BF16 C with
+ * GELU and Z); everything else on an mma.sync kernel.  flags bit 0 forces the
+ * mma.sync kernel.
  */
 ONEKA_API int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B, int32_t ldb,
                               int32_t b_kmajor, void* C, int32_t ldc, int32_t c_f32, const float* bias,
                               int32_t gelu, void* Z, int32_t M, int32_t N, int32_t K, int32_t splitk,
-                              void* stream);
+                              int32_t flags, void* stream);
+
+/* 1 when oneka_gemm_bf16 with these arguments runs on the tcgen05 kernel, else 0 (host only). */
+ONEKA_API int oneka_gemm_bf16_path(int32_t a_kmajor, int32_t b_kmajor, int32_t K, int32_t splitk, int32_t c_f32,
+                                   int32_t gelu, int32_t has_z, int32_t sigsum, int32_t flags);
+
+/*
+ * The tcgen05 kernel's device status: *code = 0, or 1 when a wait inside it
+ * timed out (the kernel then skipped its stores); reading clears it.
+ * Synchronizes the device.
+ */
+ONEKA_API int oneka_gemm_tc_status(int32_t* code);
 
 /*
  * out[n] += sum over m of sigmoid((A B^T)[m][n] + bias[n]) for k-major A [M][lda]
@@ -342,7 +358,7 @@ ONEKA_API int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, cons
  */
 ONEKA_API int oneka_gemm_bf16_sigmoid_colsum(const void* A, int32_t lda, const void* B, int32_t ldb,
                                              const float* bias, float* out, int32_t M, int32_t N, int32_t K,
-                                             void* stream);
+                                             int32_t flags, void* stream);
 
 /*
  * Binary cross-entropy of logits [B][ncells] (FP32) against chronicle masks

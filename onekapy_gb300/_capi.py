@@ -28,7 +28,8 @@ EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_r
            "oneka_track_noalloc", "oneka_track_batched", "oneka_track_batched_scratch_bytes",
            "oneka_gaussian_filter", "oneka_count_histogram", "oneka_gemm_bf16", "oneka_bce_bitmask",
            "oneka_gelu_backward", "oneka_colsum_bf16", "oneka_adamw", "oneka_features",
-           "oneka_sigmoid_colsum", "oneka_gemm_bf16_sigmoid_colsum"]
+           "oneka_sigmoid_colsum", "oneka_gemm_bf16_sigmoid_colsum", "oneka_gemm_bf16_path",
+           "oneka_gemm_tc_status"]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
@@ -127,7 +128,11 @@ def load() -> ctypes.CDLL:
         L.oneka_count_histogram.restype = ctypes.c_int
         L.oneka_count_histogram.argtypes = [_P, ctypes.c_int64, _I, _P, _P]
         L.oneka_gemm_bf16.restype = ctypes.c_int
-        L.oneka_gemm_bf16.argtypes = [_P, _I, _I, _P, _I, _I, _P, _I, _I, _P, _I, _P, _I, _I, _I, _I, _P]
+        L.oneka_gemm_bf16.argtypes = [_P, _I, _I, _P, _I, _I, _P, _I, _I, _P, _I, _P, _I, _I, _I, _I, _I, _P]
+        L.oneka_gemm_bf16_path.restype = ctypes.c_int
+        L.oneka_gemm_bf16_path.argtypes = [_I] * 9
+        L.oneka_gemm_tc_status.restype = ctypes.c_int
+        L.oneka_gemm_tc_status.argtypes = [ctypes.POINTER(ctypes.c_int32)]
         L.oneka_bce_bitmask.restype = ctypes.c_int
         L.oneka_bce_bitmask.argtypes = [_P, _P, ctypes.c_int64, _I, _I, _I, _I, ctypes.c_float, _P, _P, _P]
         L.oneka_gelu_backward.restype = ctypes.c_int
@@ -142,7 +147,7 @@ def load() -> ctypes.CDLL:
         L.oneka_sigmoid_colsum.restype = ctypes.c_int
         L.oneka_sigmoid_colsum.argtypes = [_P, _I, _I, _P, _P]
         L.oneka_gemm_bf16_sigmoid_colsum.restype = ctypes.c_int
-        L.oneka_gemm_bf16_sigmoid_colsum.argtypes = [_P, _I, _P, _I, _P, _P, _I, _I, _I, _P]
+        L.oneka_gemm_bf16_sigmoid_colsum.argtypes = [_P, _I, _P, _I, _P, _P, _I, _I, _I, _I, _P]
         L.oneka_evaluate.restype = ctypes.c_int
         L.oneka_evaluate.argtypes = [ctypes.POINTER(OnekaSite), _P, _D, _D, _D,
                                      ctypes.POINTER(ctypes.c_double), _P, ctypes.c_int64, _I, _P, _P,

@@ -36,6 +36,7 @@ UNITS = {
     "probe.cu": ["--fmad=true"],
     "noalloc.cu": ["--fmad=false"],
     "mlp.cu": ["--fmad=true"],
+    "gemm_tc.cu": ["--fmad=true"],
 }
 
 

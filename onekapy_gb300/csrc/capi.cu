@@ -26,7 +26,9 @@ cudaError_t launch_histogram(const int32_t* counts, long long n, int nbins, unsi
                              cudaStream_t s);
 cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B, int ldb, int b_kmajor, void* C,
                              int ldc, int c_f32, const float* bias, int gelu, void* Z, int M, int N, int K,
-                             int splitk, float* sigsum, cudaStream_t s);
+                             int splitk, float* sigsum, int flags, cudaStream_t s);
+int gemm_path(int a_kmajor, int b_kmajor, int K, int splitk, int c_f32, int gelu, void* Z, float* sigsum, int flags);
+cudaError_t gemm_tc_take_error(int* code);
 cudaError_t launch_bce_bitmask(const float* logits, const uint32_t* masks, long long slot_words, int wpr, int ncols,
                                int B, int ncells, float scale, void* dlogits, float* loss, cudaStream_t s);
 cudaError_t launch_gelu_backward(const float* dh, const void* z, void* dz, long long n, cudaStream_t s);
@@ -394,28 +396,44 @@ static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B, int32_t ldb, int32_t b_kmajor,
                     void* C, int32_t ldc, int32_t c_f32, const float* bias, int32_t gelu, void* Z, int32_t M,
-                    int32_t N, int32_t K, int32_t splitk, void* stream) {
+                    int32_t N, int32_t K, int32_t splitk, int32_t flags, void* stream) {
     g_err[0] = 0;
     ONEKA_CHECK_ARG(A && B && C && M > 0 && N > 0 && K > 0, "A/B/C/M/N/K");
     ONEKA_CHECK_ARG(K % 32 == 0, "K must be a multiple of 32");
     ONEKA_CHECK_ARG(lda % 8 == 0 && ldb % 8 == 0 && ldc % 8 == 0, "leading dimensions must be multiples of 8");
-    ONEKA_CHECK_ARG(al16(A) && al16(B) && al16(C) && (!Z || al16(Z)), "16-byte aligned matrices");
+    ONEKA_CHECK_ARG(al16(A) && al16(B) && al16(C) && (!Z || al16(Z)) && (!bias || al16(bias)),
+                    "16-byte aligned matrices and bias");
     ONEKA_CHECK_ARG(lda >= (a_kmajor ? K : M) && ldb >= (b_kmajor ? K : N) && ldc >= N, "leading dimensions");
     ONEKA_CHECK_ARG(splitk <= 1 || (c_f32 && !gelu && !Z), "split-K needs an FP32 output without GELU");
     ONEKA_CHECK_CUDA(launch_gemm_bf16(A, lda, a_kmajor, B, ldb, b_kmajor, C, ldc, c_f32, bias, gelu, Z, M, N, K,
-                                      splitk, nullptr, (cudaStream_t)stream));
+                                      splitk, nullptr, flags, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_gemm_bf16_path(int32_t a_kmajor, int32_t b_kmajor, int32_t K, int32_t splitk, int32_t c_f32, int32_t gelu,
+                         int32_t has_z, int32_t sigsum, int32_t flags) {
+    return gemm_path(a_kmajor, b_kmajor, K, splitk, c_f32, gelu, has_z ? (void*)1 : nullptr,
+                     sigsum ? (float*)1 : nullptr, flags);
+}
+
+int oneka_gemm_tc_status(int32_t* code) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(code, "code");
+    int c = 0;
+    ONEKA_CHECK_CUDA(gemm_tc_take_error(&c));
+    *code = c;
     return ONEKA_OK;
 }
 
 int oneka_gemm_bf16_sigmoid_colsum(const void* A, int32_t lda, const void* B, int32_t ldb, const float* bias,
-                                   float* out, int32_t M, int32_t N, int32_t K, void* stream) {
+                                   float* out, int32_t M, int32_t N, int32_t K, int32_t flags, void* stream) {
     g_err[0] = 0;
     ONEKA_CHECK_ARG(A && B && out && M > 0 && N > 0 && K > 0, "A/B/out/M/N/K");
     ONEKA_CHECK_ARG(K % 32 == 0, "K must be a multiple of 32");
     ONEKA_CHECK_ARG(lda % 8 == 0 && ldb % 8 == 0 && lda >= K && ldb >= K, "leading dimensions");
-    ONEKA_CHECK_ARG(al16(A) && al16(B), "16-byte aligned matrices");
+    ONEKA_CHECK_ARG(al16(A) && al16(B) && (!bias || al16(bias)), "16-byte aligned matrices and bias");
     ONEKA_CHECK_CUDA(launch_gemm_bf16(A, lda, 1, B, ldb, 1, nullptr, N, 1, bias, 0, nullptr, M, N, K, 1, out,
-                                      (cudaStream_t)stream));
+                                      flags, (cudaStream_t)stream));
     return ONEKA_OK;
 }
 

@@ -1,0 +1,474 @@
+// gemm_tc.cu -- the surrogate's BF16 GEMM on the 5th-generation tensor cores.
+//
+// C[M][N] = A[M][K] * B[N][K]^T (both operands K-major, BF16; FP32
+// accumulation) for the layers of the surrogate MLP, with fused epilogues:
+// bias + FP32 store (logits), bias + GELU storing the pre-activation and the
+// activation in BF16 (hidden layers), and bias + sigmoid summed over the rows
+// (the screened capture field; C is never stored).
+//
+// A persistent, warp-specialized kernel: one CTA per SM walks 128 x 256
+// output tiles (M fastest, so consecutive tiles reuse the same B slice from
+// L2).
+//   * warp 0 (one lane): TMA producer.  cp.async.bulk.tensor with the 128-byte
+//     swizzle stages 64-wide K slices of A (128 x 64) and B (256 x 64) into a
+//     4-stage shared-memory ring; "full" mbarriers complete on the copies'
+//     transaction bytes.
+//   * warp 1 (one lane): MMA issuer.  tcgen05.mma (kind::f16, M = 128,
+//     N = 256, K = 16) accumulates a tile in one of two 256-column FP32
+//     buffers of tensor memory; tcgen05.commit releases each ring stage
+//     ("empty") once its MMAs have read it, and hands a finished
+//     accumulator to the epilogue ("acc_full").
+//   * warps 2-17: epilogue.  Warp w reads TMEM lane quadrant w % 4 (tile rows
+//     32 (w % 4) ..) and one 64-column block of the tile with tcgen05.ld,
+//     applies the epilogue, and frees the buffer ("acc_empty"), so the
+//     epilogue of one tile overlaps the MMAs of the next.  Sixteen warps keep
+//     the epilogue's latencies (TMEM loads, the sigmoid, the column-sum
+//     shuffles) hidden.
+// Every mbarrier wait is bounded by the global timer: on a timeout the
+// kernel records an error, waits (bounded) for its own copies and MMAs in
+// flight, frees its tensor memory and returns.
+//
+// No counterpart in the reference (the surrogate is this project's own).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "oneka_internal.cuh"
+
+namespace oneka {
+
+__device__ int g_tc_error;   // first failure code of a tensor-core GEMM (0: none)
+
+namespace {
+
+constexpr int TM = 128, TN = 256, TK = 64, STAGES = 4;
+constexpr int EPI_WARPS = 16;                 // 4 per TMEM lane quadrant, 64 columns each
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
+constexpr int A_BYTES = TM * TK * 2;          // 16 KB
+constexpr int B_BYTES = TN * TK * 2;          // 32 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + alignment slack (1024-byte swizzle atoms)
+constexpr int TMEM_COLS = 512;       // two 256-column accumulators
+constexpr unsigned long long kWaitNs = 2000000000ull;      // 2 s per wait
+
+enum TcEpilogue { kEpiF32 = 0, kEpiGelu = 1, kEpiSigsum = 2 };
+
+struct TcArgs {
+    void* C;              // kEpiF32: float [M][ldc]; kEpiGelu: bf16 H [M][ldc]
+    __nv_bfloat16* Z;     // kEpiGelu: bf16 pre-activation [M][ldc]
+    const float* bias;    // [N] or null
+    float* sigsum;        // kEpiSigsum: out[N] += sum over rows of sigmoid
+    int M, N, K, ldc;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for phase `parity` of an mbarrier, at most kWaitNs; false on timeout
+// or when another role of the CTA has already given up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 0;; ++it) {
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            if (*abort_flag) return false;
+            if (global_ns() - t0 > kWaitNs) {
+                *abort_flag = 1;
+                atomicCAS(&g_tc_error, 0, 1);
+                return false;
+            }
+        }
+    }
+}
+
+// Teardown wait: bounded by time only (the CTA has already given up; this
+// only lets its own copies and MMAs land before the memory they use goes away).
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 0;; ++it) {
+        if (mbar_try(bar, parity)) return;
+        if ((it & 255u) == 255u && global_ns() - t0 > kWaitNs) return;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with the
+// 128-byte swizzle: rows of 128 bytes (64 BF16), 8-row swizzle atoms of
+// 1024 bytes (stride-dimension offset), version 1, swizzle mode 2 (128 B).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);            // start address
+    d |= (uint64_t)(16u >> 4) << 16;                    // leading-dimension offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024u >> 4) << 32;                  // stride-dimension offset
+    d |= 1ull << 46;                                    // descriptor version
+    d |= 2ull << 61;                                    // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = TN, M = TM.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                            ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ float gelu_tc(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+
+// Sum 16 column values over the warp's 32 lanes (rows): recursive halving,
+// 16 shuffles; returns the total of column (8 b4 + 4 b3 + 2 b2 + b1) in
+// every lane, b_i the lane's bits.
+__device__ __forceinline__ float warp_colsum16(float (&v)[16], int lane) {
+#pragma unroll
+    for (int half = 8, bit = 16; half >= 1; half >>= 1, bit >>= 1) {
+        const bool up = (lane & bit) != 0;
+#pragma unroll
+        for (int j = 0; j < half; ++j) {
+            const float send = up ? v[j] : v[j + half];
+            const float keep = up ? v[j + half] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, bit);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(THREADS, 1)
+    gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs g) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], drain;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    __shared__ int issued, consumed;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN, tiles = mt * nt;
+    const int ktiles = g.K / TK;
+    unsigned char* base = tc_smem + ((1024u - (smem_addr(tc_smem) & 1023u)) & 1023u);
+    const uint32_t sA = smem_addr(base), sB = sA + STAGES * A_BYTES;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_addr(&full[s]), 1);
+            mbar_init(smem_addr(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_addr(&acc_full[b]), 1);
+            mbar_init(smem_addr(&acc_empty[b]), EPI_WARPS);     // one arrival per epilogue warp
+        }
+        mbar_init(smem_addr(&drain), 1);
+        abort_flag = 0;
+        issued = consumed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(&tmem_base)), "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    volatile int* abort_v = &abort_flag;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: TMA slices of A and B into the ring, tile after tile
+            int it = 0;
+            for (int t = blockIdx.x; t < tiles && !*abort_v; t += gridDim.x) {
+                const int m0 = (t % mt) * TM, n0 = (t / mt) * TN;
+                int kt = 0;
+                for (; kt < ktiles; ++kt, ++it) {
+                    const int s = it % STAGES;
+                    if (it >= STAGES && !mbar_wait(smem_addr(&empty[s]), ((it / STAGES) - 1) & 1, abort_v)) break;
+                    const uint32_t bar = smem_addr(&full[s]);
+                    mbar_expect_tx(bar, STAGE_BYTES);
+                    tma_load_2d(sA + s * A_BYTES, &tmA, kt * TK, m0, bar);
+                    tma_load_2d(sB + s * B_BYTES, &tmB, kt * TK, n0, bar);
+                    issued = it + 1;
+                }
+                if (kt < ktiles) break;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer: tile tl of this CTA accumulates in buffer tl & 1
+            int it = 0, tl = 0;
+            for (int t = blockIdx.x; t < tiles && !*abort_v; t += gridDim.x, ++tl) {
+                const int b = tl & 1, u = tl >> 1;
+                if (tl >= 2 && !mbar_wait(smem_addr(&acc_empty[b]), (u - 1) & 1, abort_v)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + (uint32_t)(b * TN);
+                int kt = 0;
+                for (; kt < ktiles; ++kt, ++it) {
+                    const int s = it % STAGES;
+                    if (!mbar_wait(smem_addr(&full[s]), (it / STAGES) & 1, abort_v)) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint64_t ad = sw128_desc(sA + s * A_BYTES), bd = sw128_desc(sB + s * B_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < TK / 16; ++kk)   // +32 bytes of K per MMA: +2 in the encoded address
+                        mma_bf16(acc, ad + 2 * kk, bd + 2 * kk, (kt | kk) != 0);
+                    mma_commit(smem_addr(&empty[s]));
+                    consumed = it + 1;
+                }
+                if (kt < ktiles) break;
+                mma_commit(smem_addr(&acc_full[b]));   // fires when the tile's MMAs have completed
+            }
+            if (*abort_v) {                          // let every MMA issued above land
+                mma_commit(smem_addr(&drain));
+                mbar_drain(smem_addr(&drain), 0);
+            }
+        }
+    } else {
+        // epilogue warps 2..17: TMEM lane quadrant q = warp % 4 (tile rows
+        // 32q .. 32q + 31), columns [cb, cb + 64) of the tile
+        const int q = warp & 3, cb = ((warp - 2) >> 2) * 64;
+        int tl = 0;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++tl) {
+            const int b = tl & 1, u = tl >> 1;
+            int okw = 0;
+            if (lane == 0) okw = mbar_wait(smem_addr(&acc_full[b]), u & 1, abort_v) ? 1 : 0;
+            okw = __shfl_sync(0xffffffffu, okw, 0);      // warp-uniform (tcgen05.ld is warp-collective)
+            if (!okw) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int m0 = (t % mt) * TM, n0 = (t / mt) * TN;
+            const int row = m0 + q * 32 + lane;
+            const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TN);
+#pragma unroll 1
+            for (int c = cb; c < cb + 64; c += 16) {
+                const int nc = n0 + c;
+                if (nc >= g.N) break;                        // uniform across the warp
+                const bool whole = nc + 16 <= g.N;
+                float v[16];
+                tmem_ld16(trow + c, v);
+                if (g.bias) {
+                    if (whole) {
+                        const float4* bp = reinterpret_cast<const float4*>(g.bias + nc);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const float4 bb = __ldg(bp + j);
+                            v[4 * j] += bb.x; v[4 * j + 1] += bb.y; v[4 * j + 2] += bb.z; v[4 * j + 3] += bb.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (nc + j < g.N) v[j] += __ldg(g.bias + nc + j);
+                    }
+                }
+                if (EPI == kEpiSigsum) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = row < g.M ? 1.0f / (1.0f + __expf(-v[j])) : 0.0f;
+                    const float sum = warp_colsum16(v, lane);
+                    const int col = nc + 8 * ((lane >> 4) & 1) + 4 * ((lane >> 3) & 1) + 2 * ((lane >> 2) & 1) +
+                                    ((lane >> 1) & 1);
+                    if ((lane & 1) == 0 && col < g.N) atomicAdd(g.sigsum + col, sum);
+                } else if (row < g.M) {
+                    const long long off = (long long)row * g.ldc + nc;
+                    if (EPI == kEpiF32) {
+                        float* Cp = reinterpret_cast<float*>(g.C) + off;
+                        if (whole) {
+#pragma unroll
+                            for (int j = 0; j < 16; j += 4)
+                                *reinterpret_cast<float4*>(Cp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 16; ++j)
+                                if (nc + j < g.N) Cp[j] = v[j];
+                        }
+                    } else {
+                        __nv_bfloat16* H = reinterpret_cast<__nv_bfloat16*>(g.C) + off;
+                        __nv_bfloat16* Z = g.Z + off;
+                        if (whole) {
+                            uint32_t zp[8], hp[8];
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                const __nv_bfloat162 z2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                                const __nv_bfloat162 h2 =
+                                    __floats2bfloat162_rn(gelu_tc(v[2 * j]), gelu_tc(v[2 * j + 1]));
+                                zp[j] = *reinterpret_cast<const uint32_t*>(&z2);
+                                hp[j] = *reinterpret_cast<const uint32_t*>(&h2);
+                            }
+                            uint4* zq = reinterpret_cast<uint4*>(Z);
+                            uint4* hq = reinterpret_cast<uint4*>(H);
+                            zq[0] = make_uint4(zp[0], zp[1], zp[2], zp[3]);
+                            zq[1] = make_uint4(zp[4], zp[5], zp[6], zp[7]);
+                            hq[0] = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+                            hq[1] = make_uint4(hp[4], hp[5], hp[6], hp[7]);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                if (nc + j < g.N) {
+                                    Z[j] = __float2bfloat16(v[j]);
+                                    H[j] = __float2bfloat16(gelu_tc(v[j]));
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&acc_empty[b]));
+        }
+    }
+
+    // teardown: nothing of ours may still be in flight when the tensor memory
+    // is freed and the CTA exits
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort_v) {
+        for (int k = consumed; k < issued; ++k)      // copies not yet consumed by an MMA
+            mbar_drain(smem_addr(&full[k % STAGES]), (k / STAGES) & 1);
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+int sm_count() {
+    static int n[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (n[dev] == 0) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        n[dev] = v > 0 ? v : 148;
+    }
+    return n[dev];
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// 2-D K-major BF16 operand [rows][ld] with a box of `box_rows` x 64.
+bool make_map(CUtensorMap* map, const void* ptr, int rows, int k, int ld, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2u};
+    const cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1u, 1u};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Whether the tensor-core path takes this GEMM: K-major A and B, K a
+// multiple of 64, no split-K.
+bool gemm_tc_eligible(int a_kmajor, int b_kmajor, int K, int splitk) {
+    return a_kmajor && b_kmajor && K % TK == 0 && K > 0 && splitk <= 1 && encode_fn() != nullptr;
+}
+
+// epi: 0 FP32 C, 1 GELU (C = H bf16, Z bf16), 2 sigmoid column sums into sigsum.
+cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int epi, const float* bias,
+                           void* Z, float* sigsum, int M, int N, int K, cudaStream_t s) {
+    CUtensorMap ta, tb;
+    if (!make_map(&ta, A, M, K, lda, TM) || !make_map(&tb, B, N, K, ldb, TN)) return cudaErrorInvalidValue;
+    TcArgs g;
+    g.C = C;
+    g.Z = (__nv_bfloat16*)Z;
+    g.bias = bias;
+    g.sigsum = sigsum;
+    g.M = M; g.N = N; g.K = K; g.ldc = ldc;
+    const int tiles = ((N + TN - 1) / TN) * ((M + TM - 1) / TM);
+    dim3 grid(tiles < sm_count() ? tiles : sm_count());
+#define ONEKA_TC_CASE(E)                                                                                    \
+    {                                                                                                       \
+        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                             SMEM_BYTES);                                                   \
+        if (e != cudaSuccess) return e;                                                                     \
+        gemm_tc_kernel<E><<<grid, THREADS, SMEM_BYTES, s>>>(ta, tb, g);                                     \
+    }
+    if (epi == kEpiF32) ONEKA_TC_CASE(kEpiF32)
+    else if (epi == kEpiGelu) ONEKA_TC_CASE(kEpiGelu)
+    else ONEKA_TC_CASE(kEpiSigsum)
+#undef ONEKA_TC_CASE
+    return cudaGetLastError();
+}
+
+// Read and clear the device error flag of the tensor-core GEMM (synchronizes).
+cudaError_t gemm_tc_take_error(int* code) {
+    int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(code, g_tc_error, sizeof(int));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int));
+}
+
+}  // namespace oneka

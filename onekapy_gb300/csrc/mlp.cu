@@ -316,9 +316,27 @@ unsigned grid_for(long long n, int per) {
 
 }  // namespace
 
+bool gemm_tc_eligible(int a_kmajor, int b_kmajor, int K, int splitk);
+cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int epi, const float* bias,
+                           void* Z, float* sigsum, int M, int N, int K, cudaStream_t s);
+
+// Which kernel a GEMM runs on: 1 the tcgen05 kernel (gemm_tc.cu), 0 the
+// mma.sync kernel below.  The tcgen05 kernel takes K-major operands with K a
+// multiple of 64 and no split-K, for the FP32, GELU and sigmoid-sum
+// epilogues; bit 0 of `flags` forces the mma.sync kernel.
+int gemm_path(int a_kmajor, int b_kmajor, int K, int splitk, int c_f32, int gelu, void* Z, float* sigsum, int flags) {
+    if (flags & 1) return 0;
+    if (!gemm_tc_eligible(a_kmajor, b_kmajor, K, splitk)) return 0;
+    if (sigsum) return 1;
+    if (gelu) return (!c_f32 && Z) ? 1 : 0;
+    return c_f32 ? 1 : 0;
+}
+
 cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B, int ldb, int b_kmajor, void* C,
                              int ldc, int c_f32, const float* bias, int gelu, void* Z, int M, int N, int K,
-                             int splitk, float* sigsum, cudaStream_t s) {
+                             int splitk, float* sigsum, int flags, cudaStream_t s) {
+    if (gemm_path(a_kmajor, b_kmajor, K, splitk, c_f32, gelu, Z, sigsum, flags))
+        return launch_gemm_tc(A, lda, B, ldb, C, ldc, sigsum ? 2 : (gelu ? 1 : 0), bias, Z, sigsum, M, N, K, s);
     GemmArgs g;
     g.A = (const __nv_bfloat16*)A;
     g.B = (const __nv_bfloat16*)B;

@@ -37,13 +37,32 @@ def _p(t):
     return C.ptr(t)
 
 
-def gemm(A, a_kmajor, B, b_kmajor, C_out, M, N, K, *, bias=None, gelu=False, Z=None, splitk=1, stream=None):
+# flags of oneka_gemm_bf16: bit 0 forces the mma.sync kernel (default: the
+# tcgen05 kernel wherever it applies).
+GEMM_FLAGS = 0
+
+
+def gemm(A, a_kmajor, B, b_kmajor, C_out, M, N, K, *, bias=None, gelu=False, Z=None, splitk=1, stream=None,
+         flags=None):
     lda = A.shape[-1]
     ldb = B.shape[-1]
     ldc = C_out.shape[-1]
     C.check(C.load().oneka_gemm_bf16(_p(A), lda, int(a_kmajor), _p(B), ldb, int(b_kmajor), _p(C_out), ldc,
                                      int(C_out.dtype == F32), _p(bias), int(gelu), _p(Z), M, N, K, splitk,
-                                     C.stream_ptr(stream)))
+                                     GEMM_FLAGS if flags is None else flags, C.stream_ptr(stream)))
+
+
+def gemm_path(a_kmajor, b_kmajor, K, *, splitk=1, c_f32=True, gelu=False, has_z=False, sigsum=False, flags=None):
+    """1 when the GEMM runs on the tcgen05 kernel, 0 on the mma.sync kernel."""
+    return int(C.load().oneka_gemm_bf16_path(int(a_kmajor), int(b_kmajor), K, splitk, int(c_f32), int(gelu),
+                                             int(has_z), int(sigsum), GEMM_FLAGS if flags is None else flags))
+
+
+def tc_status() -> int:
+    """Device status of the tcgen05 GEMM (0 ok, 1 a wait timed out); clears it."""
+    v = ctypes.c_int32(0)
+    C.check(C.load().oneka_gemm_tc_status(ctypes.byref(v)))
+    return int(v.value)
 
 
 @dataclass
@@ -156,7 +175,7 @@ class MLP:
         L = self.layers[-1]
         C.check(C.load().oneka_gemm_bf16_sigmoid_colsum(_p(h), h.shape[-1], _p(L.wb), L.wb.shape[-1], _p(L.b),
                                                         _p(out), X.shape[0], L.w.shape[0], L.w.shape[1],
-                                                        C.stream_ptr()))
+                                                        GEMM_FLAGS, C.stream_ptr()))
 
 
 # ---------------------------------------------------------------------------

@@ -14,9 +14,13 @@ from onekapy_gb300 import sites as S  # noqa: E402
 from onekapy_gb300 import surrogate as SG  # noqa: E402
 
 
+@pytest.mark.parametrize("flags", [0, 1])
 @pytest.mark.parametrize("a_kmajor,b_kmajor", [(True, True), (True, False), (False, True), (False, False)])
-@pytest.mark.parametrize("M,N,K,splitk", [(256, 384, 96, 1), (200, 72, 64, 1), (128, 512, 1024, 8)])
-def test_gemm_layouts_match_fp32(a_kmajor, b_kmajor, M, N, K, splitk):
+@pytest.mark.parametrize("M,N,K,splitk", [(256, 384, 96, 1), (200, 72, 64, 1), (128, 512, 1024, 8),
+                                          (296, 520, 512, 1), (64, 65536, 512, 1)])
+def test_gemm_layouts_match_fp32(flags, a_kmajor, b_kmajor, M, N, K, splitk):
+    """Both GEMM kernels (tcgen05 where it applies, and the forced mma.sync
+    kernel) against an FP32 product of the same BF16 operands."""
     dev = C.device()
     g = torch.Generator(device="cpu").manual_seed(M + N + K)
     A = torch.randn((M, K), generator=g).to(dev)
@@ -25,22 +29,29 @@ def test_gemm_layouts_match_fp32(a_kmajor, b_kmajor, M, N, K, splitk):
     Ab = (A if a_kmajor else A.T.contiguous()).to(torch.bfloat16).contiguous()
     Bb = (B.T.contiguous() if b_kmajor else B).to(torch.bfloat16).contiguous()
     Cf = torch.zeros((M, N), dtype=torch.float32, device=dev)
-    SG.gemm(Ab, a_kmajor, Bb, b_kmajor, Cf, M, N, K, bias=bias, splitk=splitk)
+    SG.gemm(Ab, a_kmajor, Bb, b_kmajor, Cf, M, N, K, bias=bias, splitk=splitk, flags=flags)
     ref = (Ab.float() if a_kmajor else Ab.float().T) @ (Bb.float().T if b_kmajor else Bb.float())
     if bias is not None:
         ref = ref + bias
-    assert torch.allclose(Cf, ref, rtol=1e-3, atol=1e-3 * math.sqrt(K))
+    tc = SG.gemm_path(a_kmajor, b_kmajor, K, splitk=splitk, flags=flags)
+    assert tc == int(flags == 0 and a_kmajor and b_kmajor and K % 64 == 0 and splitk == 1)
+    assert SG.tc_status() == 0
+    assert torch.allclose(Cf, ref, rtol=1e-3, atol=1e-3 * math.sqrt(K)), float((Cf - ref).abs().max())
 
 
-def test_gemm_gelu_epilogue():
+@pytest.mark.parametrize("flags", [0, 1])
+@pytest.mark.parametrize("M,N,K", [(256, 128, 64), (200, 520, 512)])
+def test_gemm_gelu_epilogue(flags, M, N, K):
     dev = C.device()
-    g = torch.Generator(device="cpu").manual_seed(3)
-    A = torch.randn((256, 64), generator=g).to(dev).to(torch.bfloat16)
-    W = torch.randn((128, 64), generator=g).to(dev).to(torch.bfloat16)
-    b = torch.randn(128, generator=g).to(dev)
-    H = torch.empty((256, 128), dtype=torch.bfloat16, device=dev)
+    g = torch.Generator(device="cpu").manual_seed(3 + K)
+    A = torch.randn((M, K), generator=g).to(dev).to(torch.bfloat16)
+    W = (torch.randn((N, K), generator=g) / math.sqrt(K)).to(dev).to(torch.bfloat16)
+    b = torch.randn(N, generator=g).to(dev)
+    H = torch.empty((M, N), dtype=torch.bfloat16, device=dev)
     Z = torch.empty_like(H)
-    SG.gemm(A, True, W, True, H, 256, 128, 64, bias=b, gelu=True, Z=Z)
+    SG.gemm(A, True, W, True, H, M, N, K, bias=b, gelu=True, Z=Z, flags=flags)
+    assert SG.gemm_path(True, True, K, c_f32=False, gelu=True, has_z=True, flags=flags) == int(flags == 0)
+    assert SG.tc_status() == 0
     z = A.float() @ W.float().T + b
     assert torch.allclose(Z.float(), z, rtol=2e-2, atol=2e-2)
     assert torch.allclose(H.float(), torch.nn.functional.gelu(z), rtol=2e-2, atol=2e-2)
@@ -93,18 +104,20 @@ def test_adamw_matches_restatement():
     assert torch.equal(wb, wd.to(torch.bfloat16))
 
 
-def test_fused_sigmoid_colsum_matches_fp32():
+@pytest.mark.parametrize("flags", [0, 1])
+def test_fused_sigmoid_colsum_matches_fp32(flags):
     dev = C.device()
     g = torch.Generator(device="cpu").manual_seed(11)
-    for M, N, K in [(300, 520, 64), (2048, 4096, 256)]:
+    for M, N, K in [(300, 520, 64), (2048, 4096, 256), (130, 65536, 512)]:
         H = torch.randn((M, K), generator=g).to(dev).to(torch.bfloat16)
         W = (torch.randn((N, K), generator=g) * 0.2).to(dev).to(torch.bfloat16)
         b = torch.randn(N, generator=g).to(dev)
         out = torch.full((N,), 0.5, dtype=torch.float32, device=dev)
         C.check(C.load().oneka_gemm_bf16_sigmoid_colsum(C.ptr(H), K, C.ptr(W), K, C.ptr(b), C.ptr(out), M, N, K,
-                                                        C.stream_ptr()))
+                                                        flags, C.stream_ptr()))
+        assert SG.tc_status() == 0
         ref = 0.5 + torch.sigmoid(H.float() @ W.float().T + b).sum(0)
-        assert torch.allclose(out, ref, rtol=1e-4, atol=1e-3 * math.sqrt(M))
+        assert torch.allclose(out, ref, rtol=1e-4, atol=1e-3 * math.sqrt(M)), float((out - ref).abs().max())
 
 
 def test_trained_surrogate_screens_faster_within_tolerance():
