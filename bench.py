@@ -54,8 +54,8 @@ METRIC = "realizations/s & particle-steps/s on 1 GB300 vs plain FP64; L∞ captu
 UNIT = "realizations/s"
 SEED = 20261203
 # DRAM bytes per realization of the tracking launch on this site, from one ncu
-# capture of a 1,000-realization launch (15.62 MB; profiles/).
-TRACK32_DRAM_BYTES_PER_REALIZATION = 15.62e6 / 1000
+# capture of a 1,000-realization launch (15.48 MB; profiles/).
+TRACK32_DRAM_BYTES_PER_REALIZATION = 15.48e6 / 1000
 
 
 def args_():
