@@ -185,7 +185,7 @@ def run_reference(a):
     from onekapy_gb300 import sites as S
     spec = S.config2(nreal=a.nreal, npaths=a.npaths)
     threads = host_threads()
-    sample = 10 * max(4, threads)
+    sample = 30 * max(4, threads)
     for _ in range(a.warmup):
         cpu_oracle_rate(spec, None, max(2, threads // 4), threads)
     rates, steps_rates, total = [], [], 0.0
@@ -346,7 +346,7 @@ def run_ours(a):
         cpu = None
         if world == 1 and not a.no_cpu_baseline:
             th = host_threads()
-            ns = 10 * max(4, th)      # about 1-2 s wall on 16 threads: 15-30 s of CPU work
+            ns = 30 * max(4, th)      # about 2 s wall on 16 threads: about 30 s of CPU work
             rate, srate, dt = cpu_oracle_rate(spec, None, ns, th)
             cpu = {"value": rate, "unit": UNIT, "cores": th, "kind": "port",
                    "sample": f"{ns} realizations x {P} paths of the workload ({dt:.1f} s wall; "
