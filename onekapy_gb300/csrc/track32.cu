@@ -19,9 +19,10 @@
 // particle from a shared counter as soon as its trace ends, so a block's
 // lanes stay busy until its last particles, and no lane waits for the
 // slowest trace of a fixed group.  The Dormand-Prince stages are folded into
-// register running sums of the tableau rows (one velocity evaluation inlined
-// in a loop over the six stages); the cold per-particle state (bounding box,
-// counters, frame, vertex count) sits in shared-memory columns, one per lane.
+// register running sums of the tableau rows (the six velocity evaluations of
+// an attempt are unrolled, so every row index is a compile-time constant);
+// the cold per-particle state (bounding box, counters, frame, vertex count)
+// sits in shared-memory columns, one per lane.
 #include <math.h>
 
 #include "oneka_internal.cuh"
@@ -418,8 +419,8 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
     float ex = c_dp_e[0] * s.k1x, ey = c_dp_e[0] * s.k1y;
     float kx = 0.0f, ky = 0.0f;
     bool wet = true;
-#pragma unroll 1
-    for (int st = 0; st < 6; ++st) {            // evaluates k2..k7
+#pragma unroll
+    for (int st = 0; st < 6; ++st) {            // evaluates k2..k7 (unrolled: stage rows are compile-time)
         // px[st] selected with compile-time indexes only
         float ax = px[0], ay = py[0];
 #pragma unroll
