@@ -31,7 +31,7 @@ namespace oneka {
 namespace {
 
 struct Model32 {
-    const float4* w;     // per well: x, y (relative to the target), -q/(2 pi), q/(4 pi)
+    const float4* w;     // per well: x, y (relative to the target), -q/(2 pi), q ln(2)/(4 pi)
     int nw;
     float ox, oy;        // regional origin relative to the target
     float c0, c1, c2, c3, c4, c5;
@@ -70,7 +70,7 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
         const float s = __fdividef(w.z, r2);
         qx.add(s * dx);
         qy.add(s * dy);
-        if (!CONFINED) pot.add(w.w * __logf(r2));
+        if (!CONFINED) pot.add(w.w * __log2f(r2));     // q/(4 pi) ln r^2, ln 2 folded into w.w
     }
     if (CONFINED) {
         kx = -((qx.s - qx.c) * m.inv_hn);
@@ -535,7 +535,8 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
     for (int i = threadIdx.x; i < L.nwells; i += BLOCK) {
         const double q = L.q[(long long)r * L.nwells + i];
         w[i] = make_float4((float)(L.wells[3 * i] - L.xt), (float)(L.wells[3 * i + 1] - L.yt),
-                           (float)(-q * 0.15915494309189535), (float)(q * 0.07957747154594767));
+                           (float)(-q * 0.15915494309189535),
+                           (float)(q * (0.07957747154594767 * 0.69314718055994531)));
     }
     window_clear(ch);
     __syncthreads();
