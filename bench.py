@@ -565,8 +565,9 @@ def run_config4(a):
     ms, clocks = _timed(step32, a, stream, flush)
     n64 = min(a.fp64_sample or R, R)
     sub = real.slice(0, n64)
+    o32h = E.TrackOptions(**{**o32.__dict__, "head64": True})
     res = {}
-    for name, o in (("fp32", o32), ("fp64", o64)):
+    for name, o in (("fp32", o32), ("fp64", o64), ("fp32_head64", o32h)):
         c = torch.zeros_like(counts)
         out = E.TrackOutputs.alloc(n64, P, dev, endpoint=True, stats=True, counters=True)
         torch.cuda.synchronize()
@@ -578,6 +579,17 @@ def run_config4(a):
         res[name] = (c, out, e0.elapsed_time(e1) / 1e3)
     c32, out32, t32 = res["fp32"]
     c64, out64, t64 = res["fp64"]
+
+    def vs64(c, out):
+        d = (c - c64).abs().double() / n64
+        okp = (out.status == C.TRACE_OK) & (out64.status == C.TRACE_OK)
+        dr = ((out.endpoint - out64.endpoint).norm(dim=-1) / spec.spacing)[okp]
+        qq = torch.quantile(dr.float(), torch.tensor([0.5, 0.99], device=dev)).tolist() if dr.numel() else [0, 0]
+        return {"linf_capture_probability": float(d.max().item()), "cells_above_0.01": int((d > 0.01).sum().item()),
+                "drift_p50_cells": qq[0], "drift_p99_cells": qq[1],
+                "drift_max_cells": float(dr.max().item()) if dr.numel() else 0.0}
+
+    c32h, out32h, t32h = res["fp32_head64"]
     diff = (c32 - c64).abs().double() / n64
     visited = (c64 > 0) | (c32 > 0)
     ok = (out32.status == C.TRACE_OK) & (out64.status == C.TRACE_OK)
@@ -604,6 +616,9 @@ def run_config4(a):
                                        if drift.numel() else 1.0,
                                        "particles_compared": int(drift.numel())},
                  status_agreement=status_agree,
+                 fp32_head64={"note": "general path with heads within 1 % of the aquifer top re-inverted in FP64",
+                              "seconds_fp64_sample": t32h, "seconds_fp32_sample": t32,
+                              "vs_fp64": vs64(c32h, out32h), "fp32_vs_fp64": vs64(c32, out32)},
                  tracker_launch={"block": o32.block, "occupancy": o32.occupancy, "window_kb": o32.window_kb},
                  clocks=clocks)
     print(json.dumps(line))

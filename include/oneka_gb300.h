@@ -132,6 +132,9 @@ typedef struct OnekaTrackOpts {
     int32_t window_kb;       /* shared-memory chronicle window per block in KiB (0: 32; < 0: none) */
     int32_t occupancy;       /* FP32 build: resident blocks per SM to compile for (4, 6, 8 at 128
                                 threads; 2, 3 at 256); 0: the lowest */
+    int32_t head64;          /* FP32 build, general path: 1 re-inverts a head within 1 % of the
+                                aquifer top in FP64 from the compensated potential (off: FP32);
+                                runs the 256 x 3 launch shape; not for batched launches */
 } OnekaTrackOpts;
 
 /* Optional per-particle outputs ([nreal][npaths] leading); any pointer may be NULL. */

@@ -63,7 +63,7 @@ class OnekaFrame(ctypes.Structure):
 class OnekaTrackOpts(ctypes.Structure):
     _fields_ = [("duration", _D), ("tol", _D), ("maxstep", _D), ("umbra", _D), ("confined", _I),
                 ("precision", _I), ("max_attempts", _I), ("block", _I), ("window_kb", _I),
-                ("occupancy", _I)]
+                ("occupancy", _I), ("head64", _I)]
 
 
 class OnekaTrackOut(ctypes.Structure):

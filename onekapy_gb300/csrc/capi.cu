@@ -278,6 +278,7 @@ int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void* scratch,
         const int rc = check_track_args(J.site, J.real, J.nreal, J.release, J.npaths, J.opts, J.grid, J.out);
         if (rc != ONEKA_OK) return rc;
         ONEKA_CHECK_ARG(J.opts->precision == ONEKA_FP32, "batched launches run the FP32 build");
+        ONEKA_CHECK_ARG(!J.opts->head64, "batched launches do not take head64");
         ONEKA_CHECK_ARG(J.counts, "counts");
     }
     cudaStream_t s = (cudaStream_t)stream;

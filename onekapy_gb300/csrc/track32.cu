@@ -40,6 +40,7 @@ struct Model32 {
     float kh2f;          // 0.5 K H^2
     float inv_k;         // 1 / K
     float inv_kh;        // 1 / (K H)
+    const double* d64;   // {K, n, H} in FP64 (read only by the near-top inversion of kGeneralHead64)
 };
 
 struct Kahan {
@@ -52,8 +53,13 @@ struct Kahan {
     }
 };
 
-template <bool CONFINED>
+// Velocity modes of the FP32 build: the general (mixed) path, the confined
+// path, and the general path with the optional FP64 near-top head inversion.
+enum Mode32 { kGeneral = 0, kConfined = 1, kGeneralHead64 = 2 };
+
+template <int MODE>
 __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, float& kx, float& ky) {
+    constexpr bool CONFINED = MODE == kConfined;
     const float dxo = x - m.ox;
     const float dyo = y - m.oy;
     Kahan qx{-(2.0f * m.c0 * dxo + m.c2 * dyo + m.c3), 0.0f};
@@ -89,8 +95,17 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
     const float kh2 = m.kh2f;
     const float hu = sqrtf(fmaxf(2.0f * phi * m.inv_k, 0.0f));
     const float hc = (phi + kh2) * m.inv_kh;
-    const float head = (phi < kh2) ? hu : hc;
-    const float inv = (head > m.H) ? m.inv_hn : __fdividef(1.0f, head * m.n);
+    float head = (phi < kh2) ? hu : hc;
+    float inv = (head > m.H) ? m.inv_hn : __fdividef(1.0f, head * m.n);
+    if (MODE == kGeneralHead64 && fabsf(head - m.H) < 0.01f * m.H) {
+        // optional: the inversion in FP64 from the unrounded compensated pair
+        // (model.py:341-350 operation order)
+        const double K = m.d64[0], n = m.d64[1], H = m.d64[2];
+        const double ph = (double)pot.s - (double)pot.c;
+        const double h = (ph < 0.5 * K * H * H) ? sqrt(2.0 * ph / K) : (ph + 0.5 * K * H * H) / (K * H);
+        head = (float)h;
+        inv = (h > H) ? m.inv_hn : (float)(1.0 / (h * n));
+    }
     kx = -((qx.s - qx.c) * inv);
     ky = -((qy.s - qy.c) * inv);
     return (phi > 0.0f) && (head > 0.0f);
@@ -263,6 +278,7 @@ __constant__ float c_dp_e[7] = {(float)DP::e1, 0.0f, (float)DP::e3, (float)DP::e
 
 struct RealConst32 {
     float c0, c1, c2, c3, c4, c5, K, n, H, inv_hn, ox, oy, kh2f, inv_k, inv_kh;
+    double d64[3];       // K, n, H in FP64 for the optional near-top head inversion
     float tol, maxstep;  // options, converted once
     Raster32 g;          // grid constants of the chronicle
     int skip;
@@ -301,7 +317,7 @@ struct Cold {
 };
 
 // The realization's constants come from shared memory (block-uniform).
-template <bool CONFINED>
+template <int MODE>
 __device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* w, int nw, float x, float y,
                                         float& kx, float& ky) {
     Model32 m;
@@ -311,7 +327,8 @@ __device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* w, 
     m.c0 = rc.c0; m.c1 = rc.c1; m.c2 = rc.c2; m.c3 = rc.c3; m.c4 = rc.c4; m.c5 = rc.c5;
     m.K = rc.K; m.n = rc.n; m.H = rc.H; m.inv_hn = rc.inv_hn; m.kh2f = rc.kh2f;
     m.inv_k = rc.inv_k; m.inv_kh = rc.inv_kh;
-    return feval32<CONFINED>(m, x, y, kx, ky);
+    m.d64 = rc.d64;
+    return feval32<MODE>(m, x, y, kx, ky);
 }
 
 // Write the finished particle's outputs.
@@ -351,7 +368,7 @@ __device__ __forceinline__ void push_vertex(const TrackLaunch& L, int r, const P
 // Start particle s.p: release point, frame, first velocity (k1).  Returns
 // false when the trace is already over (dry at the release point, or a zero
 // duration).
-template <bool CONFINED, int BLOCK>
+template <int MODE, int BLOCK>
 __device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealConst32& rc, const float4* w,
                                         Particle32& s, const Cold<BLOCK>& c) {
     const double rx = L.release[2 * s.p] - L.xt, ry = L.release[2 * s.p + 1] - L.yt;
@@ -382,7 +399,7 @@ __device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealC
     c.f(kBy0) = c.f(kBy1) = s.yh + s.yl;
     push_vertex<BLOCK>(L, r, s, c);
     float kx, ky;
-    if (!feval_c<CONFINED>(rc, w, L.nwells, s.xh + s.xl, s.yh + s.yl, kx, ky)) {
+    if (!feval_c<MODE>(rc, w, L.nwells, s.xh + s.xl, s.yh + s.yl, kx, ky)) {
         s.status = ONEKA_TRACE_DRY;
         return false;
     }
@@ -393,7 +410,7 @@ __device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealC
 
 // One step attempt of the Dormand-Prince integrator (capturezone.py:221-247).
 // Returns false when the trace is over.
-template <bool CONFINED, int BLOCK>
+template <int MODE, int BLOCK>
 __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst32& rc, const float4* w,
                                           const Chron& ch, Particle32& s, int r, const Cold<BLOCK>& c) {
     if (s.att >= L.max_attempts) {
@@ -427,7 +444,7 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
         for (int q = 1; q < 6; ++q)
             if (q == st) { ax = px[q]; ay = py[q]; }
         // a dry stage ends the trace after the attempt (nothing of it is kept)
-        wet &= feval_c<CONFINED>(rc, w, L.nwells, s.xh + (s.xl + dt * ax), s.yh + (s.yl + dt * ay), kx, ky);
+        wet &= feval_c<MODE>(rc, w, L.nwells, s.xh + (s.xl + dt * ax), s.yh + (s.yl + dt * ay), kx, ky);
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             px[q] += c_dp_b[st][q] * kx;
@@ -492,7 +509,7 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
 }
 
 // One block: realization k of launch L (wave-local), particles of chunk blockIdx.x.
-template <bool CONFINED, int BLOCK>
+template <int MODE, int BLOCK>
 __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks) {
     extern __shared__ float4 sm32[];
     __shared__ RealConst32 rc;
@@ -516,6 +533,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
         rc.kh2f = (float)(0.5 * Kd * (Hd * Hd));
         rc.inv_k = (float)(1.0 / Kd);
         rc.inv_kh = (float)(1.0 / (Kd * Hd));
+        rc.d64[0] = Kd; rc.d64[1] = nd; rc.d64[2] = Hd;
         rc.tol = (float)L.opts.tol;
         rc.maxstep = (float)L.opts.maxstep;
         rc.g.dx = (float)L.grid.dx;
@@ -551,27 +569,27 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
     bool live = false;
     // start this lane's first particle; a lane whose trace ends at once takes the next
     while (s.p < pend && !live) {
-        live = start32<CONFINED, BLOCK>(L, r, rc, w, s, cold);
+        live = start32<MODE, BLOCK>(L, r, rc, w, s, cold);
         if (!live) {
             finish32<BLOCK>(L, r, s, cold, ch);
             s.p = atomicAdd(&rc.next, 1);
         }
     }
     while (live) {
-        live = attempt32<CONFINED, BLOCK>(L, rc, w, ch, s, r, cold);
+        live = attempt32<MODE, BLOCK>(L, rc, w, ch, s, r, cold);
         while (!live && s.p < pend) {
             finish32<BLOCK>(L, r, s, cold, ch);
             s.p = atomicAdd(&rc.next, 1);
-            if (s.p < pend) live = start32<CONFINED, BLOCK>(L, r, rc, w, s, cold);
+            if (s.p < pend) live = start32<MODE, BLOCK>(L, r, rc, w, s, cold);
         }
     }
     __syncthreads();
     window_flush(ch);
 }
 
-template <bool CONFINED, int BLOCK, int MINB>
+template <int MODE, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) track32_kernel(const TrackLaunch L, int chunks) {
-    block32<CONFINED, BLOCK>(L, blockIdx.y, chunks);
+    block32<MODE, BLOCK>(L, blockIdx.y, chunks);
 }
 
 // Many sites in one launch: row blockIdx.y belongs to job j with
@@ -590,12 +608,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) track32_batch_kernel(const __grid
     const TrackLaunch& J = T.job[lo];
     const int k = row - T.first[lo];
     if (J.opts.confined)
-        block32<true, BLOCK>(J, k, chunks);
+        block32<kConfined, BLOCK>(J, k, chunks);
     else
-        block32<false, BLOCK>(J, k, chunks);
+        block32<kGeneral, BLOCK>(J, k, chunks);
 }
 
-template <bool CONFINED, int BLOCK, int MINB>
+template <int MODE, int BLOCK, int MINB>
 cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
     static int sms = 0;
     if (!sms) {
@@ -615,26 +633,26 @@ cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
     }
     const size_t smem = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)kColdFields * BLOCK +
                         4 * (size_t)L.win_rows * L.win_words;
-    auto kern = track32_kernel<CONFINED, BLOCK, MINB>;
+    auto kern = track32_kernel<MODE, BLOCK, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<dim3((unsigned)chunks, (unsigned)L.nr), BLOCK, smem, s>>>(L, chunks);
     return cudaGetLastError();
 }
 
-template <bool CONFINED>
-cudaError_t launch_confined(const TrackLaunch& L, cudaStream_t s) {
+template <int MODE>
+cudaError_t launch_mode(const TrackLaunch& L, cudaStream_t s) {
     // (threads per block, minimum resident blocks per SM): the variants the
     // autotuner chooses between through OnekaTrackOpts.block / .occupancy
     const int block = L.opts.block > 0 ? L.opts.block : 256;
     const int occ = L.opts.occupancy;
-    if (block == 64) return launch_variant<CONFINED, 64, 8>(L, s);
-    if (block == 256) return occ >= 3 ? launch_variant<CONFINED, 256, 3>(L, s)
-                                      : launch_variant<CONFINED, 256, 2>(L, s);
-    if (block == 32) return launch_variant<CONFINED, 32, 16>(L, s);
-    if (occ >= 8) return launch_variant<CONFINED, 128, 8>(L, s);
-    if (occ >= 6) return launch_variant<CONFINED, 128, 6>(L, s);
-    return launch_variant<CONFINED, 128, 4>(L, s);
+    if (block == 64) return launch_variant<MODE, 64, 8>(L, s);
+    if (block == 256) return occ >= 3 ? launch_variant<MODE, 256, 3>(L, s)
+                                      : launch_variant<MODE, 256, 2>(L, s);
+    if (block == 32) return launch_variant<MODE, 32, 16>(L, s);
+    if (occ >= 8) return launch_variant<MODE, 128, 8>(L, s);
+    if (occ >= 6) return launch_variant<MODE, 128, 6>(L, s);
+    return launch_variant<MODE, 128, 4>(L, s);
 }
 
 template <int BLOCK, int MINB>
@@ -666,7 +684,10 @@ cudaError_t launch_batch_variant(const JobTable& T, int rows, size_t smem, cudaS
 }  // namespace
 
 cudaError_t launch_track32(const TrackLaunch& L, cudaStream_t s) {
-    return L.opts.confined ? launch_confined<true>(L, s) : launch_confined<false>(L, s);
+    if (L.opts.confined) return launch_mode<kConfined>(L, s);
+    // the FP64 near-top head inversion is compiled for the default launch shape only
+    if (L.opts.head64) return launch_variant<kGeneralHead64, 256, 3>(L, s);
+    return launch_mode<kGeneral>(L, s);
 }
 
 cudaError_t launch_track32_batch(const JobTable& T, int rows, cudaStream_t s) {

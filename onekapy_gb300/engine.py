@@ -285,12 +285,13 @@ class TrackOptions:
     block: int = 0
     window_kb: int = 0
     occupancy: int = 0
+    head64: bool = False
 
     def c(self) -> C.OnekaTrackOpts:
         return C.OnekaTrackOpts(float(self.duration), float(self.tol), float(self.maxstep),
                                 float(self.umbra), int(bool(self.confined)), int(self.precision),
                                 int(self.max_attempts), int(self.block), int(self.window_kb),
-                                int(self.occupancy))
+                                int(self.occupancy), int(bool(self.head64)))
 
 
 @dataclass

@@ -21,12 +21,13 @@ def golden_grid(d, key="grid"):
     return E.Grid(float(g[0]), float(g[1]), float(g[2]), float(g[3]), int(g[4]), int(g[5]))
 
 
-def golden_opts(d, precision):
+def golden_opts(d, precision, head64=False):
     return E.TrackOptions(duration=float(d["duration"]), tol=float(d["tol"]), maxstep=float(d["maxstep"]),
-                          umbra=float(d["umbra"]), confined=bool(d["confined"]), precision=precision)
+                          umbra=float(d["umbra"]), confined=bool(d["confined"]), precision=precision,
+                          head64=head64)
 
 
-def run_golden(d, precision, max_vertices=None, slots=None):
+def run_golden(d, precision, max_vertices=None, slots=None, head64=False):
     dev = C.device()
     site = golden_site(d, dev)
     real = golden_real(d, dev)
@@ -36,7 +37,7 @@ def run_golden(d, precision, max_vertices=None, slots=None):
     out = E.TrackOutputs.alloc(nreal, npaths, dev, bbox=True, max_vertices=mv)
     counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
     reg = torch.zeros(1, dtype=torch.int64, device=dev)
-    E.track(site, real, torch.as_tensor(d["release"], device=dev), golden_opts(d, precision), grid,
+    E.track(site, real, torch.as_tensor(d["release"], device=dev), golden_opts(d, precision, head64), grid,
             counts=counts, registered=reg, outputs=out, slots=slots)
     torch.cuda.synchronize()
     return dict(counts=counts.cpu().numpy(), registered=int(reg.item()),

@@ -22,12 +22,12 @@ def _oracle_counts(oracle_mod, site, real, spec, grid, frames=None, nthreads=0):
                             xo=site.xo, yo=site.yo, frames=frames, nthreads=nthreads)
 
 
-def _gpu_counts(site, real, spec, grid, precision, outputs=None):
+def _gpu_counts(site, real, spec, grid, precision, outputs=None, head64=False):
     dev = site.device
     counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
     reg = torch.zeros(1, dtype=torch.int64, device=dev)
     opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
-                          confined=spec.confined, precision=precision)
+                          confined=spec.confined, precision=precision, head64=head64)
     E.track(site, real, torch.as_tensor(site.release(spec.npaths), device=dev), opts, grid,
             counts=counts, registered=reg, outputs=outputs)
     torch.cuda.synchronize()
@@ -119,12 +119,13 @@ def test_config4_subset_fp64_vs_oracle_and_fp32(oracle_mod):
     want = _oracle_counts(oracle_mod, site, real, spec, grid)
     assert reg == int(ok.sum())
     assert np.array_equal(got, want["counts"]), f"{(got != want['counts']).sum()} nodes differ"
-    out32 = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
-    got32, _ = _gpu_counts(site, real, spec, grid, C.FP32, outputs=out32)
-    same = (out32.naccept == out64.naccept).cpu().numpy() & (out64.status == 0).cpu().numpy()
-    drift = (out32.endpoint - out64.endpoint).abs().amax(dim=2).cpu().numpy()[same]
-    assert np.percentile(drift, 99) <= 1e-3 * spec.spacing, np.percentile(drift, 99)
-    assert np.abs(got32 - got).max() / max(reg, 1) <= 0.1
+    for head64 in (False, True):      # FP32 head inversion, and the FP64 one near the aquifer top
+        out32 = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
+        got32, _ = _gpu_counts(site, real, spec, grid, C.FP32, outputs=out32, head64=head64)
+        same = (out32.naccept == out64.naccept).cpu().numpy() & (out64.status == 0).cpu().numpy()
+        drift = (out32.endpoint - out64.endpoint).abs().amax(dim=2).cpu().numpy()[same]
+        assert np.percentile(drift, 99) <= 1e-3 * spec.spacing, (head64, np.percentile(drift, 99))
+        assert np.abs(got32 - got).max() / max(reg, 1) <= 0.1
 
 
 def test_create_stochastic_capturezone_dropin(oracle_mod):
