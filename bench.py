@@ -61,7 +61,7 @@ TRACK32_DRAM_BYTES_PER_REALIZATION = 15.48e6 / 1000
 def args_():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nreal", type=int, default=10000)
@@ -87,7 +87,7 @@ def workload_config(spec, a, world):
 
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -105,7 +105,7 @@ class ClockSampler:
         os.close(fd)
         self.out = open(self.path, "w")
         self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                      "-i", str(self.index), "-lms", "200"], stdout=self.out,
+                                      "-i", str(self.index), "-lms", "50"], stdout=self.out,
                                      stderr=subprocess.DEVNULL)
 
     def stop(self):
@@ -263,10 +263,11 @@ def run_ours(a):
     for _ in range(a.warmup):
         step(o32, R)
     torch.cuda.synchronize()
-    cnt = E.TrackOutputs(counters=torch.zeros(4, dtype=torch.int64, device=dev))
+    cnt = E.TrackOutputs(counters=torch.zeros(E.COUNTERS, dtype=torch.int64, device=dev))
     step(o32, R, outputs=cnt)
     torch.cuda.synchronize()
-    attempts, accepts, ntests, natoms = (int(v) for v in cnt.counters.cpu().tolist())
+    counters = [int(v) for v in cnt.counters.cpu().tolist()]
+    attempts, accepts, ntests, natoms = counters[:4]
     counts32_full = counts.clone()
 
     # timed region
@@ -363,8 +364,7 @@ def run_ours(a):
                              "speedup_fp32_over_fp64": value / world / fp64_rate},
                 "fp32_vs_fp64": {"linf_capture_probability": linf, "mismatched_visited_fraction": mism,
                                  "sample_realizations": n64},
-                "work_per_step": {"step_attempts": attempts, "accepted_steps": accepts,
-                                  "chronicle_node_tests": ntests, "chronicle_word_atomics": natoms},
+                "work_per_step": dict(zip(E.COUNTER_NAMES[:7], counters[:7])),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak / 1e12,
                              "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
                              "traffic": TRACK32_DRAM_BYTES_PER_REALIZATION * R,
@@ -499,7 +499,7 @@ def run_config3(a):
     batched = [j.counts.clone() for j in jobs]
     # work counters (untimed pass)
     for j in jobs:
-        j.outputs = E.TrackOutputs(counters=torch.zeros(4, dtype=torch.int64, device=dev))
+        j.outputs = E.TrackOutputs(counters=torch.zeros(E.COUNTERS, dtype=torch.int64, device=dev))
     body()
     torch.cuda.synchronize()
     accepts = sum(int(j.outputs.counters[1].item()) for j in jobs)

@@ -148,8 +148,10 @@ typedef struct OnekaTrackOut {
     int32_t* nvertices;      /* vertices in the full trace (may exceed max_vertices) */
     int32_t max_vertices;
     int32_t pad;
-    int64_t* counters;       /* [4] summed over all particles: step attempts, accepted steps,
-                                chronicle node tests, chronicle word atomics; or NULL */
+    int64_t* counters;       /* [8] summed over all particles: step attempts, accepted steps,
+                                chronicle node tests, chronicle word ORs, DRY traces, STEP_LIMIT
+                                traces, traces reaching the grid's outer nodes (clipped by a fixed
+                                window; the reference would expand its grid), 0; or NULL */
 } OnekaTrackOut;
 
 /* ---------------------------------------------------------------------- */

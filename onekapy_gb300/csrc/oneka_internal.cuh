@@ -241,14 +241,25 @@ __device__ __forceinline__ void note_rows(uint32_t* slot, long long mwords, int 
     atomicMax(slot + mwords + 1, (uint32_t)(rhi + 1));
 }
 
-// Per-thread work counters, added into OnekaTrackOut.counters at the end.
+// Per-particle counters, added into OnekaTrackOut.counters when the trace
+// ends: [0] step attempts, [1] accepted steps, [2] chronicle node tests,
+// [3] chronicle word ORs, [4] DRY traces, [5] STEP_LIMIT traces, [6] traces
+// that left the grid (their bounding box reaches the grid's outer nodes,
+// where the reference's ProbabilityField.expand would grow the grid,
+// oneka/probabilityfield.py:228-244; a fixed window clips them), [7] 0.
 __device__ __forceinline__ void add_counters(long long* c, long long att, long long acc, long long ntest,
-                                             long long natom) {
+                                             long long natom, int status, const OnekaGrid& g, double bx0,
+                                             double bx1, double by0, double by1) {
     if (!c) return;
-    atomicAdd((unsigned long long*)c + 0, (unsigned long long)att);
-    atomicAdd((unsigned long long*)c + 1, (unsigned long long)acc);
-    atomicAdd((unsigned long long*)c + 2, (unsigned long long)ntest);
-    atomicAdd((unsigned long long*)c + 3, (unsigned long long)natom);
+    unsigned long long* u = (unsigned long long*)c;
+    atomicAdd(u + 0, (unsigned long long)att);
+    atomicAdd(u + 1, (unsigned long long)acc);
+    atomicAdd(u + 2, (unsigned long long)ntest);
+    atomicAdd(u + 3, (unsigned long long)natom);
+    if (status == ONEKA_TRACE_DRY) atomicAdd(u + 4, 1ull);
+    if (status == ONEKA_TRACE_STEP_LIMIT) atomicAdd(u + 5, 1ull);
+    const double xmax = g.xmin + (g.ncols - 1) * g.dx, ymax = g.ymin + (g.nrows - 1) * g.dy;
+    if (bx0 <= g.xmin || bx1 >= xmax || by0 <= g.ymin || by1 >= ymax) atomicAdd(u + 6, 1ull);
 }
 
 }  // namespace oneka

@@ -351,7 +351,10 @@ __device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Part
     if (L.out.status) L.out.status[idx] = s.status;
     if (L.out.nvertices) L.out.nvertices[idx] = c.i(kNv);
     note_rows(ch.slot, L.mask_words, L.grid.nrows, c.i(kRlo), c.i(kRhi));
-    add_counters((long long*)L.out.counters, s.att, c.i(kAcc), (unsigned)c.i(kNtest), (unsigned)c.i(kNatom));
+    if (L.out.counters)
+        add_counters((long long*)L.out.counters, s.att, c.i(kAcc), (unsigned)c.i(kNtest), (unsigned)c.i(kNatom),
+                     s.status, L.grid, L.xt + (double)c.f(kBx0), L.xt + (double)c.f(kBx1), L.yt + (double)c.f(kBy0),
+                     L.yt + (double)c.f(kBy1));
 }
 
 template <int BLOCK>

@@ -246,7 +246,8 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
     if (L.out.status) L.out.status[idx] = status;
     if (L.out.nvertices) L.out.nvertices[idx] = vs.n;
     note_rows(slot, L.mask_words, L.grid.nrows, rlo, rhi);
-    add_counters((long long*)L.out.counters, att, acc, ntest, natom);
+    add_counters((long long*)L.out.counters, att, acc, ntest, natom, status, L.grid, vs.bx0, vs.bx1, vs.by0,
+                 vs.by1);
 }
 
 }  // namespace

@@ -294,6 +294,13 @@ class TrackOptions:
                                 int(self.occupancy), int(bool(self.head64)))
 
 
+# OnekaTrackOut.counters: attempts, accepted steps, node tests, word ORs, DRY
+# traces, STEP_LIMIT traces, traces that left the grid, (reserved)
+COUNTERS = 8
+COUNTER_NAMES = ("step_attempts", "accepted_steps", "chronicle_node_tests", "chronicle_word_ors", "dry_traces",
+                 "step_limit_traces", "traces_leaving_grid", "reserved")
+
+
 @dataclass
 class TrackOutputs:
     """Per-particle outputs [nreal, npaths] (any subset)."""
@@ -319,7 +326,7 @@ class TrackOutputs:
             vertices=(torch.full(shp + (max_vertices, 2), float("nan"), dtype=F64, device=device)
                       if max_vertices else None),
             nvertices=torch.zeros(shp, dtype=I32, device=device) if (stats or max_vertices) else None,
-            counters=torch.zeros(4, dtype=torch.int64, device=device) if counters else None)
+            counters=torch.zeros(COUNTERS, dtype=torch.int64, device=device) if counters else None)
 
     def c(self) -> C.OnekaTrackOut:
         mv = 0 if self.vertices is None else int(self.vertices.shape[2])

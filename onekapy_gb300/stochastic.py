@@ -9,7 +9,14 @@ are tracked and chronicled by ``oneka_track``.
 By default the result replays the reference's auto-expanding grid exactly (a
 first pass records every trace's bounding box).  Passing ``window=half_width``
 instead fixes the grid to the square of that half width around the target
-well, the fast path for large runs: traces leaving it are clipped.
+well, the fast path for large runs: traces leaving it are clipped (counted
+in ``pfield.traces_leaving_grid``).
+
+A fixed-window run can be checkpointed: ``checkpoint=path`` saves the counts
+after every chunk of realizations and resumes from a saved state of the same
+inputs; ``max_chunks`` stops after that many chunks (``pfield.complete`` is
+then False) so that a later call continues the run.  The resumed counts equal
+those of an uninterrupted run.
 """
 from __future__ import annotations
 
@@ -17,6 +24,7 @@ import numpy as np
 import torch
 
 from . import _capi as C
+from . import checkpoint as CK
 from . import engine as E
 from .engine import DistributionError, Lognormal
 from .probabilityfield import ProbabilityField
@@ -37,8 +45,10 @@ def create_stochastic_capturezone(
         stochastic_wells, observations,
         spacing, umbra, confined,
         tol, maxstep, *, seed=0, precision=C.FP64, window=None, chunk=4096,
-        mode=C.MODE_STOCHASTIC):
+        mode=C.MODE_STOCHASTIC, checkpoint=None, max_chunks=None):
     """Stochastic capture zone of the target well (oneka/stochastic.py:76-270)."""
+    if checkpoint is not None and window is None:
+        raise ValueError("checkpoint needs a fixed window (the auto-expanding grid is known only at the end)")
     dev = C.device()
     site = E.Site(stochastic_wells, observations, base, target=target, c_dist=c_dist, p_dist=p_dist,
                   t_dist=t_dist, device=dev)
@@ -71,20 +81,47 @@ def create_stochastic_capturezone(
             pfield.expand(bb[:, 0].min(), bb[:, 1].max(), bb[:, 2].min(), bb[:, 3].max())
         frames = frames_np
         grid = pfield._grid()
+    state = None
+    first = 0
     counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
     registered = torch.zeros(1, dtype=torch.int64, device=dev)
-    for a in range(0, nrealizations, chunk):
+    if checkpoint is not None:
+        sig = CK.signature(target=target, npaths=npaths, duration=duration, nrealizations=nrealizations,
+                           base=base, c_dist=c_dist, p_dist=p_dist, t_dist=t_dist,
+                           stochastic_wells=stochastic_wells, observations=observations, spacing=spacing,
+                           umbra=umbra, confined=confined, tol=tol, maxstep=maxstep, seed=seed,
+                           precision=precision, window=window, mode=mode)
+        state = CK.open_state(checkpoint, sig, (grid.nrows, grid.ncols), nrealizations)
+        counts.copy_(torch.from_numpy(state.counts))
+        registered.fill_(state.registered)
+        first = state.next_realization
+    counters = torch.zeros(E.COUNTERS, dtype=torch.int64, device=dev)
+    out = E.TrackOutputs(counters=counters)
+    done_chunks = 0
+    a = first
+    while a < nrealizations and (max_chunks is None or done_chunks < max_chunks):
         b = min(nrealizations, a + chunk)
         fr = None
         if frames is not None and npaths > 0:
             fr = torch.frombuffer(bytearray(frames[a * npaths:b * npaths].tobytes()),
                                   dtype=torch.uint8).to(dev)
         E.track(site, real.slice(a, b), release, opts, grid, counts=counts, registered=registered,
-                frames=fr)
+                frames=fr, outputs=out)
+        a = b
+        done_chunks += 1
+        if state is not None:
+            state.counts = counts.cpu().numpy()
+            state.registered = int(registered.item())
+            state.next_realization = a
+            state.save(checkpoint)
     pfield.counts = counts
     pfield.pgrid = counts.to(torch.float64)
     pfield.total_weight = float(registered.item())
     pfield.realizations = real
+    pfield.complete = a >= nrealizations
+    c = counters.cpu().tolist()
+    pfield.trace_counters = dict(zip(E.COUNTER_NAMES[:7], c[:7]))
+    pfield.traces_leaving_grid = int(c[6])
     return pfield
 
 

@@ -163,3 +163,26 @@ def test_deterministic_capturezone_runs():
     assert pf.total_weight == 1.0
     p = pf.probability()
     assert float(p.max()) == 1.0 and float(p.min()) == 0.0
+
+
+def test_checkpoint_resume_equals_uninterrupted_run(tmp_path):
+    """A fixed-window run stopped after one chunk and resumed from its
+    checkpoint gives the counts of the uninterrupted run."""
+    from onekapy_gb300.stochastic import create_stochastic_capturezone
+    spec = S.config1()
+    args = (0, 48, spec.duration, 12, spec.base, spec.c_dist, spec.p_dist, spec.t_dist, spec.wells,
+            spec.observations, spec.spacing, spec.umbra, True, spec.tol, spec.maxstep)
+    kw = dict(seed=5, precision=C.FP32, window=600.0, chunk=5)
+    full = create_stochastic_capturezone(*args, **kw)
+    assert full.complete and full.total_weight == 12.0
+    path = str(tmp_path / "run.npz")
+    part = create_stochastic_capturezone(*args, **kw, checkpoint=path, max_chunks=1)
+    assert not part.complete and part.total_weight == 5.0
+    rest = create_stochastic_capturezone(*args, **kw, checkpoint=path)
+    assert rest.complete and rest.total_weight == 12.0
+    assert torch.equal(rest.counts, full.counts)
+    done = create_stochastic_capturezone(*args, **kw, checkpoint=path)     # nothing left to do
+    assert done.complete and torch.equal(done.counts, full.counts)
+    with pytest.raises(ValueError, match="different inputs"):
+        create_stochastic_capturezone(*args, **{**kw, "seed": 6}, checkpoint=path)
+    assert full.traces_leaving_grid >= 0 and full.trace_counters["accepted_steps"] > 0

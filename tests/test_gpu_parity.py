@@ -279,3 +279,35 @@ def test_expand_known_answer_gpu():
     assert np.isclose(pf.ymin, r["ymin"]) and np.isclose(pf.ymax, r["ymax"])
     pf.expand(*KA.EXPAND_SECOND)
     assert (pf.nrows, pf.ncols) == (r["nrows"], r["ncols"])
+
+
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_trace_counters_match_per_particle_outputs(precision):
+    """OnekaTrackOut.counters against the per-particle outputs of the same
+    launch: attempts, accepted steps, DRY and STEP_LIMIT traces, and the traces
+    whose bounding box reaches the grid's outer nodes (a window smaller than
+    the traces, so that some are clipped)."""
+    d = golden("track_unconfined_dryshift.npz")
+    dev = C.device()
+    site = golden_site(d, dev)
+    real = golden_real(d, dev)
+    g0 = golden_grid(d)
+    grid = E.Grid(site.xt - 2 * g0.dx, site.yt - 2 * g0.dy, g0.dx, g0.dy, 5, 5)   # 5 x 5 nodes
+    nreal, npaths = d["nvertices"].shape
+    out = E.TrackOutputs.alloc(nreal, npaths, dev, bbox=True, counters=True)
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+    E.track(site, real, torch.as_tensor(d["release"], device=dev), golden_opts(d, precision), grid,
+            counts=counts, outputs=out)
+    torch.cuda.synchronize()
+    c = out.counters.cpu().numpy()
+    st = out.status.cpu().numpy()
+    assert c[0] == int(out.nattempt.sum().item())
+    assert c[1] == int(out.naccept.sum().item())
+    assert c[4] == int((st == C.TRACE_DRY).sum()) and c[4] > 0
+    assert c[5] == int((st == C.TRACE_STEP_LIMIT).sum())
+    bb = out.bbox.cpu().numpy().reshape(-1, 4)
+    xmax = grid.xmin + (grid.ncols - 1) * grid.dx
+    ymax = grid.ymin + (grid.nrows - 1) * grid.dy
+    left = (bb[:, 0] <= grid.xmin) | (bb[:, 1] >= xmax) | (bb[:, 2] <= grid.ymin) | (bb[:, 3] >= ymax)
+    assert c[6] == int(left.sum()) and c[6] > 0
+    assert c[7] == 0
