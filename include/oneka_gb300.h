@@ -52,6 +52,9 @@ extern "C" {
 #define ONEKA_REAL_OK 0
 #define ONEKA_REAL_RANGE 1       /* an observed head is at or below the base (model.py:558-559 RangeError) */
 #define ONEKA_REAL_NOT_SPD 2     /* normal equations not positive definite (model.py:604 LinAlgError) */
+#define ONEKA_REAL_NOT_FINITE 3  /* the fitted or drawn coefficients are not finite, e.g. an observation on a
+                                    well (log 0 in construct_fit, model.py:565); the reference would then
+                                    backtrace with NaN velocities and never end.  Not tracked. */
 
 /* per-particle status (oneka_track) */
 #define ONEKA_TRACE_OK 0         /* reached |duration| */

@@ -16,7 +16,7 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_lib", "liboneka_gb300.so")
 
 ONEKA_OK, ONEKA_ERR_INVALID, ONEKA_ERR_CUDA, ONEKA_ERR_SCRATCH = 0, -1, -2, -3
-REAL_OK, REAL_RANGE, REAL_NOT_SPD = 0, 1, 2
+REAL_OK, REAL_RANGE, REAL_NOT_SPD, REAL_NOT_FINITE = 0, 1, 2, 3
 TRACE_OK, TRACE_DRY, TRACE_STEP_LIMIT, TRACE_SKIPPED = 0, 1, 2, 3
 DIST_CONST, DIST_UNIFORM, DIST_TRIANGULAR, DIST_LOGNORMAL = 0, 1, 2, 3
 MODE_STOCHASTIC, MODE_MEAN, MODE_GIVEN, MODE_GIVEN_EV = 0, 1, 2, 3

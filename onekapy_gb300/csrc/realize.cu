@@ -270,6 +270,8 @@ __global__ void __launch_bounds__(32 * kWarps) realize_kernel(const RealizeParam
         } else {
             for (int i = 0; i < 6; ++i) coef[i] = ev[i];
         }
+        for (int i = 0; i < 6; ++i)
+            if (!isfinite(ev[i]) || !isfinite(coef[i])) status = ONEKA_REAL_NOT_FINITE;
     } else {
         for (int i = 0; i < 6; ++i)
             for (int j = 0; j < 6; ++j) cov[i][j] = NAN;

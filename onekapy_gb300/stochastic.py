@@ -37,6 +37,9 @@ def _check_status(real: E.Realizations):
         raise RangeError("model.fit_coeficient: elevation < base")
     if np.any(st == C.REAL_NOT_SPD):
         raise np.linalg.LinAlgError("normal equations are not positive definite")
+    if np.any(st == C.REAL_NOT_FINITE):
+        raise np.linalg.LinAlgError("the regional-flow fit is not finite (an observation on a well? "
+                                    "utilities.filter_obs removes observations within a buffer of the wells)")
 
 
 def create_stochastic_capturezone(

@@ -19,8 +19,18 @@ What it records (all FP64, as the reference computes):
 * ``fit_cases.npz``: ``Model.fit_regional_flow`` on synthetic observation sets.
 * ``raster_cases.npz``: ``ProbabilityField.rasterize`` on random polylines.
 * ``expand_geometry.npz``: ``ProbabilityField.expand`` geometry sequences.
+* ``site_<name>.npz``: the reference's own site files (``data/<name>.py``) run
+  through its top-level sequence: ``filter_obs`` with the site's buffer
+  (oneka/oneka.py:254), then the deterministic driver
+  (``create_deterministic_capturezone``, oneka/deterministic.py:65-235): the
+  site's inputs (distributions, mean wells and aquifer, raw and filtered
+  observations), the fitted coef_ev / coef_cov, and the auto-expanded grid's
+  geometry and counts.
 
-Synthetic sites are seeded; no reference data file is copied.
+Synthetic sites are seeded.  The site fixtures hold the numbers of the
+reference's site files as inputs next to its outputs on them.
+
+    python tests/golden/make_golden.py --only sites     # just the site fixtures
 """
 from __future__ import annotations
 
@@ -44,6 +54,55 @@ def import_reference(path):
     np.float = float        # removed from NumPy >= 1.24; the reference still names it
     from oneka import capturezone, model, probabilityfield
     return model, capturezone, probabilityfield
+
+
+SITE_FILES = ["basic", "basic_deterministic", "barnesville", "carlos", "long_prairie", "paynesville", "perham"]
+
+
+def _dist_row(d):
+    """A distribution as [kind, a, b, c]: kind 0 constant, 2 uniform (a, b), 3 triangular."""
+    if type(d) is not tuple:
+        return [0.0, float(d), 0.0, 0.0]
+    if len(d) == 2:
+        return [2.0, float(d[0]), float(d[1]), 0.0]
+    return [3.0, float(d[0]), float(d[1]), float(d[2])]
+
+
+def make_site_goldens(out, meta, names=None):
+    """The reference's deterministic capture zone of each of its site files."""
+    import importlib
+    import time
+    from oneka import deterministic, model, stochastic, utilities
+    for name in names or SITE_FILES:
+        site = importlib.import_module(f"data.{name}")
+        t0 = time.time()
+        # as the reference's top-level driver does (oneka/oneka.py:254): drop
+        # observations within the buffer of any well, then the capture zone
+        obs = utilities.filter_obs(site.OBSERVATIONS, site.WELLS, site.BUFFER)
+        pf = deterministic.create_deterministic_capturezone(
+            site.TARGET, site.NPATHS, site.DURATION, site.BASE, site.C_DIST, site.P_DIST, site.T_DIST,
+            site.WELLS, obs, site.SPACING, site.UMBRA, site.CONFINED, site.TOL, site.MAXSTEP)
+        # the driver's own fit, repeated to record its coefficients
+        mean = stochastic.compute_variate_mean
+        wells = [[w[0], w[1], w[2], mean(w[3])] for w in site.WELLS]
+        K, n, H = mean(site.C_DIST), mean(site.P_DIST), mean(site.T_DIST)
+        xt, yt, rt = site.WELLS[site.TARGET][0:3]
+        mo = model.Model(site.BASE, K, n, H, wells)
+        ev, cov = mo.fit_regional_flow(obs, xt, yt)
+        np.savez_compressed(
+            os.path.join(out, f"site_{name}.npz"),
+            wells=np.array(wells, dtype=np.float64), qdist=np.array([_dist_row(w[3]) for w in site.WELLS]),
+            obs_raw=np.array(site.OBSERVATIONS, dtype=np.float64), buffer=float(site.BUFFER),
+            obs=np.array([tuple(float(v) for v in o) for o in obs], dtype=np.float64),
+            c_dist=np.array(_dist_row(site.C_DIST)), p_dist=np.array(_dist_row(site.P_DIST)),
+            t_dist=np.array(_dist_row(site.T_DIST)), base=float(site.BASE), K=float(K), n=float(n), H=float(H),
+            coef_ev=np.reshape(ev, 6), coef_cov=np.reshape(cov, 36), target=int(site.TARGET),
+            xt=float(xt), yt=float(yt), rt=float(rt), npaths=int(site.NPATHS), duration=float(site.DURATION),
+            spacing=float(site.SPACING), umbra=float(site.UMBRA), confined=bool(site.CONFINED),
+            tol=float(site.TOL), maxstep=float(site.MAXSTEP), pgrid=pf.pgrid, xmin=pf.xmin, ymin=pf.ymin,
+            xmax=pf.xmax, ymax=pf.ymax, nrows=pf.nrows, ncols=pf.ncols, total_weight=pf.total_weight, **meta)
+        print(f"site_{name}: {len(wells)} wells, {len(obs)} of {len(site.OBSERVATIONS)} obs, grid {pf.nrows}x{pf.ncols}, "
+              f"{int(np.count_nonzero(pf.pgrid))} visited nodes, {time.time() - t0:.1f} s", flush=True)
 
 
 def import_reference_utilities():
@@ -139,10 +198,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--out", default=HERE)
+    ap.add_argument("--only", choices=["sites"], default=None)
+    ap.add_argument("--site", action="append", default=None, help="with --only sites: these site files only")
     args = ap.parse_args()
     M, C, PF = import_reference(args.reference)
     meta = dict(numpy=np.__version__, python=platform.python_version(), machine=platform.machine())
     print("reference imported;", meta)
+    make_site_goldens(args.out, meta, args.site)
+    if args.only == "sites":
+        return
 
     rng = np.random.default_rng(20260101)
     day = 365.25
