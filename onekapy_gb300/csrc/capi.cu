@@ -2,7 +2,9 @@
 #include <math.h>
 #include <stdarg.h>
 
+#include <algorithm>
 #include <memory>
+#include <vector>
 #include <stdio.h>
 #include <string.h>
 
@@ -295,8 +297,18 @@ int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void* scratch,
         off = 0;
         return ONEKA_OK;
     };
-    for (int j = 0; j < njobs; ++j) {
+    // costliest jobs first: their blocks are dispatched first, and the cheap
+    // ones fill the tail (realizations x paths x well terms x duration)
+    std::vector<int> order(njobs);
+    for (int j = 0; j < njobs; ++j) order[j] = j;
+    auto cost = [&](int j) {
         const OnekaTrackJob& J = jobs[j];
+        return (double)J.nreal * (double)J.npaths * (double)(J.site->nwells + 8) * fabs(J.opts->duration);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+    constexpr int kMaxRows = 1 << 30;
+    for (int jj = 0; jj < njobs; ++jj) {
+        const OnekaTrackJob& J = jobs[order[jj]];
         TrackLaunch base;
         fill_launch(base, J.site, J.real, J.release, J.npaths, J.opts, J.grid, nullptr, J.registered, J.out);
         base.counts = J.counts;
@@ -307,7 +319,7 @@ int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void* scratch,
         int r = 0;
         while (r < J.nreal) {
             const size_t room = off < scratch_bytes ? (scratch_bytes - off) / slot : 0;
-            if (room == 0 || n == kMaxJobs || rows == 65535) {
+            if (room == 0 || n == kMaxJobs || rows == kMaxRows) {
                 if (n == 0) {
                     set_error("scratch of %zu bytes is smaller than one realization slot (%zu bytes)",
                               scratch_bytes, slot);
@@ -319,7 +331,7 @@ int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void* scratch,
             }
             int take = J.nreal - r;
             if ((size_t)take > room) take = (int)room;
-            if (take > 65535 - rows) take = 65535 - rows;
+            if (take > kMaxRows - rows) take = kMaxRows - rows;
             TrackLaunch& L = T->job[n];
             L = base;
             L.r0 = r;

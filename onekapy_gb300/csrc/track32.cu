@@ -511,9 +511,9 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
     return s.tau_h != 0.0f;
 }
 
-// One block: realization k of launch L (wave-local), particles of chunk blockIdx.x.
+// One block: realization k of launch L (wave-local), particles of chunk `chunk`.
 template <int MODE, int BLOCK>
-__device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks) {
+__device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, int chunks) {
     extern __shared__ float4 sm32[];
     __shared__ RealConst32 rc;
     const int r = L.r0 + k;
@@ -524,7 +524,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
     const Chron ch = make_chron(L, slot, cold.base + kColdFields * BLOCK);
     // particles [pbeg, pend) of this block
     const int per = (L.npaths + chunks - 1) / chunks;
-    const int pbeg = blockIdx.x * per;
+    const int pbeg = chunk * per;
     const int pend = min(L.npaths, pbeg + per);
     if (threadIdx.x == 0) {
         const double* c = L.coef + 6LL * r;
@@ -551,7 +551,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
         rc.oy = (float)(L.yo - L.yt);
         rc.skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
         rc.next = pbeg + BLOCK;
-        if (!rc.skip && blockIdx.x == 0 && L.registered) atomicAdd(L.registered, 1ull);
+        if (!rc.skip && chunk == 0 && L.registered) atomicAdd(L.registered, 1ull);
     }
     for (int i = threadIdx.x; i < L.nwells; i += BLOCK) {
         const double q = L.q[(long long)r * L.nwells + i];
@@ -592,17 +592,20 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunks)
 
 template <int MODE, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) track32_kernel(const TrackLaunch L, int chunks) {
-    block32<MODE, BLOCK>(L, blockIdx.y, chunks);
+    block32<MODE, BLOCK>(L, blockIdx.y, blockIdx.x, chunks);
 }
 
-// Many sites in one launch: row blockIdx.y belongs to job j with
+// Many sites in one launch: row blockIdx.x belongs to job j with
 // first[j] <= row < first[j + 1]; jobs may differ in wells, paths, grid,
-// duration and aquifer type.  The table is a __grid_constant__ parameter, so
-// it is read in place (no copy) and a captured CUDA graph carries it.
+// duration and aquifer type.  blockIdx.y is the particle chunk.  Rows run
+// along x (up to 2^31 - 1 of them) and the host packs the costliest jobs
+// first, so they are dispatched first.  The table is a __grid_constant__
+// parameter, so it is read in place (no copy) and a captured CUDA graph
+// carries it.
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) track32_batch_kernel(const __grid_constant__ JobTable T,
                                                                      int chunks) {
-    const int row = blockIdx.y;
+    const int row = blockIdx.x;
     int lo = 0, hi = T.njobs - 1;
     while (lo < hi) {                       // last job with first[j] <= row
         const int mid = (lo + hi + 1) >> 1;
@@ -611,9 +614,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) track32_batch_kernel(const __grid
     const TrackLaunch& J = T.job[lo];
     const int k = row - T.first[lo];
     if (J.opts.confined)
-        block32<kConfined, BLOCK>(J, k, chunks);
+        block32<kConfined, BLOCK>(J, k, blockIdx.y, chunks);
     else
-        block32<kGeneral, BLOCK>(J, k, chunks);
+        block32<kGeneral, BLOCK>(J, k, blockIdx.y, chunks);
 }
 
 template <int MODE, int BLOCK, int MINB>
@@ -680,7 +683,7 @@ cudaError_t launch_batch_variant(const JobTable& T, int rows, size_t smem, cudaS
     auto kern = track32_batch_kernel<BLOCK, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<dim3((unsigned)chunks, (unsigned)rows), BLOCK, smem, s>>>(T, chunks);
+    kern<<<dim3((unsigned)rows, (unsigned)chunks), BLOCK, smem, s>>>(T, chunks);
     return cudaGetLastError();
 }
 
