@@ -14,7 +14,6 @@ Reference map (paths within OnekaPy):
 from __future__ import annotations
 
 import ctypes
-import math
 from dataclasses import dataclass, field
 
 import numpy as np

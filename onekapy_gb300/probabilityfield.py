@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _capi as C
-from .engine import Grid, FRAME_DTYPE
+from .engine import Grid
 
 
 class Error(Exception):

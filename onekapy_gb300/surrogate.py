@@ -23,7 +23,6 @@ import math
 import time
 from dataclasses import dataclass
 
-import numpy as np
 import torch
 
 from . import _capi as C

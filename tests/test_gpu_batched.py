@@ -1,5 +1,4 @@
 """GPU: one batched launch over uneven sites equals one oneka_track per site."""
-import numpy as np
 import pytest
 import torch
 
