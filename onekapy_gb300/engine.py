@@ -6,7 +6,8 @@ are what the reference-compatible modules (``stochastic``, ``capturezone``,
 ``deterministic``) and ``bench.py`` drive.
 
 Reference map (paths within OnekaPy):
-  oneka/stochastic.py:76-270     create_stochastic_capturezone -> Engine.run
+  oneka/stochastic.py:224-241    draws, fit, MVN draw          -> realize() (oneka_realize)
+  oneka/capturezone.py:51-253    backtrace + chronicle         -> track() (oneka_track), track_batched()
   oneka/stochastic.py:274-306    distributions                 -> dist()
   oneka/capturezone.py:110-115   release ring                  -> release_ring()
   oneka/probabilityfield.py:125-261  grid geometry             -> Grid, replay_expand()
