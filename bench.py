@@ -337,9 +337,7 @@ def run_ours(a):
             "public API and engine disagree"
 
         # roofline of the tracking kernel: algorithmic FP32 flops per launch
-        nw = len(spec.wells)
-        fv = 10 * nw + 12 + (0 if spec.confined else 6 * nw + 12)
-        flops = attempts * (6 * fv + 150) + 12 * ntests
+        flops = algorithmic_flops(len(spec.wells), spec.confined, attempts, ntests)
         t_track = float(np.mean(track_ms)) / 1e3
         peak = ctypes_peak(C, fp64=False)
         achieved = flops / t_track / 1e12
@@ -417,6 +415,25 @@ def _opts(spec, precision):
     from onekapy_gb300 import engine as E
     return E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
                           confined=spec.confined, precision=precision)
+
+
+def algorithmic_flops(nwells, confined, attempts, node_tests):
+    """FP32 flops of the tracking kernel's work: attempts x (6 F_v + 150) plus
+    12 per chronicle node test; F_v = 10 N_w + 12 (confined), 16 N_w + 24
+    (general)."""
+    fv = 10 * nwells + 12 + (0 if confined else 6 * nwells + 12)
+    return attempts * (6 * fv + 150) + 12 * node_tests
+
+
+def fp32_roofline(flops, seconds, kernel):
+    import torch
+    from onekapy_gb300 import _capi as C
+    peak = ctypes_peak(C, fp64=False)
+    torch.cuda.synchronize()
+    achieved = flops / seconds / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s",
+            "frac": achieved / (peak / 1e12), "traffic": None, "kernel": kernel,
+            "peak_source": "measured FP32 FMA loop on this GPU (oneka_fma_peak)"}
 
 
 def _line(a, value, unit, metric, config, dtype="f32", **extra):
@@ -504,6 +521,8 @@ def run_config3(a):
     torch.cuda.synchronize()
     accepts = sum(int(j.outputs.counters[1].item()) for j in jobs)
     attempts = sum(int(j.outputs.counters[0].item()) for j in jobs)
+    flops = sum(algorithmic_flops(j.site.nwells, j.opts.confined, int(j.outputs.counters[0].item()),
+                                  int(j.outputs.counters[2].item())) for j in jobs)
     for j in jobs:
         j.outputs = None
     # one call per site (realize + oneka_track), same realizations
@@ -525,6 +544,8 @@ def run_config3(a):
     line = _line(a, tot_real / t, UNIT, METRIC + " (64 uneven sites, batched)", cfg,
                  ms_per_step=1e3 * t, particle_steps_per_s=accepts / t, particles_per_s=tot_part / t,
                  work_per_step={"step_attempts": attempts, "accepted_steps": accepts},
+                 roofline=fp32_roofline(flops, t, "track32_batch_kernel (+ register_batch_kernel, realize); "
+                                                  "per-site F_v by well count"),
                  per_site_calls={"ms_per_step": ms_site[0], "realizations_per_s": tot_real / (ms_site[0] / 1e3),
                                  "batched_speedup": ms_site[0] / (1e3 * t)},
                  counts_equal_batched_vs_per_site=bool(same),
@@ -598,10 +619,14 @@ def run_config4(a):
     status_agree = float((out32.status == out64.status).double().mean().item())
     t = float(np.mean(ms)) / 1e3
     steps = int(out32.counters[1].item()) * R / n64
+    flops = algorithmic_flops(site.nwells, spec.confined, int(out32.counters[0].item()),
+                              int(out32.counters[2].item())) * R / n64
     cfg = {"workload": "config4-unconfined-31wells: 5000 realizations x 2048 paths, 25 y, 5 m grid 8x8 km",
            "nreal": R, "npaths": P, "fp64_realizations": n64, "l2": "512 MB buffer written between timed steps"}
     line = _line(a, R / t, UNIT, METRIC + " (unconfined stress)", cfg, ms_per_step=1e3 * t,
                  particle_steps_per_s=steps / t,
+                 roofline=fp32_roofline(flops, t, "track32_kernel (+ register_counts, realize); flops scaled from "
+                                                  f"the {n64}-realization counters"),
                  fp64_gpu={"realizations_per_s": n64 / t64, "speedup_fp32_over_fp64": (R / t) / (n64 / t64)},
                  fp32_vs_fp64_per_cell={"linf_capture_probability": float(diff.max().item()),
                                         "mean_abs_over_visited_cells": float(diff[visited].mean().item())
