@@ -167,3 +167,25 @@ def test_trained_surrogate_screens_faster_within_tolerance():
           f"track-all {t_track * 1e3:.1f} ms")
     assert float(err.max()) < 0.1
     assert res.seconds < t_track, (res.seconds, t_track)
+
+
+def test_untrained_surrogate_is_rejected_and_every_realization_tracked():
+    """An untrained network fails the judges (L-inf above the tolerance);
+    screen() then tracks every realization, and the field equals tracking
+    them all directly, node for node."""
+    dev = C.device()
+    spec = S.config5(npaths=200)
+    site = E.Site(spec.wells, spec.observations, spec.base, c_dist=spec.c_dist, p_dist=spec.p_dist,
+                  t_dist=spec.t_dist, device=dev)
+    grid = E.Grid(site.xt - 630.0, site.yt - 630.0, 20.0, 20.0, 64, 64)
+    release = torch.as_tensor(site.release(spec.npaths), device=dev)
+    opts = E.TrackOptions(duration=5 * 365.25, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=False, precision=C.FP32)
+    real = E.realize(site, 600, seed=21)
+    feats = SG.Features(real, site.nwells)
+    model = SG.MLP([64, 64, 64, 64 * 64], dev, seed=1, out_bias=2.0)      # sigmoid(2) = 0.88 everywhere
+    res = SG.screen(model, feats, site, real, release, opts, grid, judge_fraction=0.05, tolerance=0.05)
+    assert not res.accepted and res.judge_linf > 0.05
+    counts = torch.zeros((64, 64), dtype=torch.int32, device=dev)
+    E.track(site, real, release, opts, grid, counts=counts)
+    assert torch.equal(res.field, counts.double().reshape(64, 64) / real.n)
