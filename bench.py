@@ -370,6 +370,7 @@ def run_ours(a):
                                                "scaled by realizations (profiles/track32_config2_1000real_full.md)",
                              "kernel": "track32_kernel (+ register_counts_kernel)",
                              "peak_source": "measured FP32 FMA loop on this GPU (oneka_fma_peak)"},
+                "roofline_hbm": _hbm_roofline(TRACK32_DRAM_BYTES_PER_REALIZATION * R, t_track),
                 "e2e": {"value": e2e_n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "tracker_launch": {"block": o32.block, "occupancy": o32.occupancy,
@@ -382,6 +383,18 @@ def run_ours(a):
         dist.destroy_process_group()
     if line is not None:
         print(json.dumps(line))
+
+
+def _hbm_roofline(dram_bytes, seconds):
+    """The tracking step against HBM: its measured DRAM traffic over the
+    measured copy bandwidth (it is not memory-bound; this shows by how much)."""
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, src = 6800.0, "fallback 6.8 TB/s"
+    if os.path.exists(peaks_path):
+        peak, src = float(json.load(open(peaks_path))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs of measured"
+    achieved = dram_bytes / seconds / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": dram_bytes, "peak_source": src}
 
 
 def ctypes_peak(C, fp64):
