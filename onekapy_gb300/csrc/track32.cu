@@ -7,7 +7,8 @@
 //     the particle position is a float pair (hi + lo) updated with an
 //     error-free two-sum, so the position keeps ~48 bits over hundreds of
 //     steps;
-//   * well terms are summed with Kahan compensation (discharge and potential);
+//   * the discharge's well terms are summed with Kahan compensation (the
+//     potential's too in the FP64 head-inversion mode);
 //   * the head is inverted from the compensated potential in FP32 (the
 //     inversion is well conditioned; see feval32);
 //   * the time left is a float pair counting down to zero, so no FP64
@@ -76,7 +77,17 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
         const float s = __fdividef(w.z, r2);
         qx.add(s * dx);
         qy.add(s * dy);
-        if (!CONFINED) pot.add(w.w * __log2f(r2));     // q/(4 pi) ln r^2, ln 2 folded into w.w
+        // q/(4 pi) ln r^2 (ln 2 folded into w.w).  The discharge sums above
+        // carry the trace's accuracy and are compensated; the potential only
+        // selects the head branch and scales the velocity, and compensating
+        // it changed no measured drift, so it is compensated only where the
+        // FP64 head inversion reads the unrounded pair.
+        if (!CONFINED) {
+            if (MODE == kGeneralHead64)
+                pot.add(w.w * __log2f(r2));
+            else
+                pot.s += w.w * __log2f(r2);
+        }
     }
     if (CONFINED) {
         kx = -((qx.s - qx.c) * m.inv_hn);
