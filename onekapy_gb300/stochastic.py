@@ -20,6 +20,8 @@ those of an uninterrupted run.
 """
 from __future__ import annotations
 
+import logging
+
 import numpy as np
 import torch
 
@@ -29,6 +31,25 @@ from . import engine as E
 from .engine import DistributionError, Lognormal
 from .probabilityfield import ProbabilityField
 from .model import RangeError
+
+
+log = logging.getLogger("Oneka")
+
+
+def _log_realizations(real: E.Realizations, base: float):
+    """The reference's per-realization log lines (oneka/stochastic.py:243-250),
+    written only when the "Oneka" logger takes INFO (one copy to the host)."""
+    if not log.isEnabledFor(logging.INFO) or real.coef_ev is None:
+        return
+    coef = real.coef.cpu().numpy()
+    ev = real.coef_ev.cpu().numpy()
+    aq = real.aquifer.cpu().numpy()
+    for i in range(real.n):
+        K, n, H = aq[i]
+        c, e = coef[i], ev[i]
+        log.info("Realization #%d: %.2f, %.2f, %.2f, %.2f, %.4e", i, base, K, n, H, 2 * (c[0] + c[1]))
+        log.info("    coef ev:  (%+.4e, %+.4e, %+.4e, %+.4e, %+.4e, %+.4e)", *e)
+        log.info("    coef rng: (%+.4e, %+.4e, %+.4e, %+.4e, %+.4e, %+.4e)", *c)
 
 
 def _check_status(real: E.Realizations):
@@ -57,6 +78,8 @@ def create_stochastic_capturezone(
                   t_dist=t_dist, device=dev)
     real = E.realize(site, nrealizations, seed=seed, mode=mode)
     _check_status(real)
+    if mode == C.MODE_STOCHASTIC:
+        _log_realizations(real, base)
     opts = E.TrackOptions(duration=duration, tol=tol, maxstep=maxstep, umbra=umbra,
                           confined=confined, precision=precision)
     release = torch.as_tensor(site.release(npaths), device=dev)

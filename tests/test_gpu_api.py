@@ -186,3 +186,28 @@ def test_checkpoint_resume_equals_uninterrupted_run(tmp_path):
     with pytest.raises(ValueError, match="different inputs"):
         create_stochastic_capturezone(*args, **{**kw, "seed": 6}, checkpoint=path)
     assert full.traces_leaving_grid >= 0 and full.trace_counters["accepted_steps"] > 0
+
+
+def test_drivers_write_the_reference_log_lines(caplog):
+    """With the "Oneka" logger at INFO, the stochastic driver writes the
+    reference's three lines per realization and the deterministic driver its
+    parameter block; the logged values are the realizations' own."""
+    import logging
+    from onekapy_gb300.deterministic import create_deterministic_capturezone
+    from onekapy_gb300.stochastic import create_stochastic_capturezone
+    spec = S.config1()
+    args = (spec.base, spec.c_dist, spec.p_dist, spec.t_dist, spec.wells, spec.observations, spec.spacing,
+            spec.umbra, True, spec.tol, spec.maxstep)
+    with caplog.at_level(logging.INFO, logger="Oneka"):
+        pf = create_stochastic_capturezone(0, 16, spec.duration, 3, *args, seed=3, window=300.0)
+    lines = [r.getMessage() for r in caplog.records if r.name == "Oneka"]
+    assert len(lines) == 9 and lines[0].startswith("Realization #0: ")
+    c = pf.realizations.coef.cpu().numpy()[2]
+    assert lines[8] == "    coef rng: (" + ", ".join(f"{v:+.4e}" for v in c) + ")"
+    caplog.clear()
+    with caplog.at_level(logging.INFO, logger="Oneka"):
+        pf = create_deterministic_capturezone(0, 16, spec.duration, *args)
+    lines = [r.getMessage() for r in caplog.records if r.name == "Oneka"]
+    assert "Deterministic Capture Zone Parameters: " in lines
+    assert lines[-1] == f"F = {pf.realizations.coef.cpu().numpy()[0][5]:+.4e}"
+    assert not any(l.startswith("Realization #") for l in lines)
