@@ -39,3 +39,28 @@ def filter_obs(observations, wellfield, buffer):
             retained.append(obs[i])
         i = j
     return retained
+
+
+def summary_statistics(values, names, formats, title):
+    """Fixed-width table of count, min, median, max, mean and standard
+    deviation per column, NaNs left out (oneka/utilities.py:148-256): the text
+    the reference logs for the retained observations.  Returns an
+    io.StringIO; use .getvalue() for the string."""
+    import io
+    ncol = len(values[0])
+    widths = [len(format(1, f)) for f in formats]
+    width = 5 + sum(widths)
+    cols = []
+    for j in range(ncol):
+        x = np.array([v[j] for v in values], dtype=np.float64)
+        cols.append(x[~np.isnan(x)])
+    rows = [("min", np.min), ("med", np.median), ("max", np.max), ("avg", np.mean), ("std", np.std)]
+    out = [f"{title:^{width}s}", "=" * width,
+           "     " + "".join(f"{names[j]:>{widths[j]}s}" for j in range(ncol)), "-" * width,
+           "cnt: " + "".join(f"{len(cols[j]):>{widths[j]}d}" for j in range(ncol))]
+    for label, fn in rows:
+        out.append(f"{label}: " + "".join(format(fn(cols[j]), formats[j]) for j in range(ncol)))
+    out.append("=" * width)
+    buf = io.StringIO()
+    buf.write("\n".join(out) + "\n")
+    return buf

@@ -31,6 +31,7 @@ Synthetic sites are seeded.  The site fixtures hold the numbers of the
 reference's site files as inputs next to its outputs on them.
 
     python tests/golden/make_golden.py --only sites     # just the site fixtures
+    python tests/golden/make_golden.py --only stats     # just summary_statistics.npz
 """
 from __future__ import annotations
 
@@ -103,6 +104,34 @@ def make_site_goldens(out, meta, names=None):
             xmax=pf.xmax, ymax=pf.ymax, nrows=pf.nrows, ncols=pf.ncols, total_weight=pf.total_weight, **meta)
         print(f"site_{name}: {len(wells)} wells, {len(obs)} of {len(site.OBSERVATIONS)} obs, grid {pf.nrows}x{pf.ncols}, "
               f"{int(np.count_nonzero(pf.pgrid))} visited nodes, {time.time() - t0:.1f} s", flush=True)
+
+
+def make_stats_goldens(out, meta):
+    """utilities.summary_statistics on the retained observations of each site
+    file, as the reference's driver logs them (oneka/oneka.py:258-259), and
+    on a synthetic table with NaNs and mixed formats."""
+    import importlib
+    from oneka import utilities
+    cases = []
+    for name in SITE_FILES:
+        site = importlib.import_module(f"data.{name}")
+        obs = utilities.filter_obs(site.OBSERVATIONS, site.WELLS, site.BUFFER)
+        cases.append((np.array(obs, dtype=np.float64), ["Easting", "Northing", "Head", "Stdev"],
+                      ["12.2f", "12.2f", "12.2f", "12.2f"], "Retained Observations"))
+    rng = np.random.default_rng(5)
+    v = rng.normal(size=(40, 3)) * [1.0, 100.0, 1e-3]
+    v[[3, 17], 1] = np.nan
+    cases.append((v, ["a", "bb", "c"], ["8.3f", "10.1f", "11.3e"], "Mixed formats"))
+    fields = {}
+    for i, (vals, names, fmts, title) in enumerate(cases):
+        fields[f"values_{i}"] = vals
+        fields[f"names_{i}"] = np.array(names)
+        fields[f"formats_{i}"] = np.array(fmts)
+        fields[f"title_{i}"] = np.array(title)
+        fields[f"text_{i}"] = np.array(utilities.summary_statistics([tuple(r) for r in vals], names, fmts,
+                                                                    title).getvalue())
+    np.savez_compressed(os.path.join(out, "summary_statistics.npz"), ncases=len(cases), **fields, **meta)
+    print(f"summary_statistics.npz: {len(cases)} cases")
 
 
 def import_reference_utilities():
@@ -198,15 +227,19 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--out", default=HERE)
-    ap.add_argument("--only", choices=["sites"], default=None)
+    ap.add_argument("--only", choices=["sites", "stats"], default=None)
     ap.add_argument("--site", action="append", default=None, help="with --only sites: these site files only")
     args = ap.parse_args()
     M, C, PF = import_reference(args.reference)
     meta = dict(numpy=np.__version__, python=platform.python_version(), machine=platform.machine())
     print("reference imported;", meta)
+    if args.only == "stats":
+        make_stats_goldens(args.out, meta)
+        return
     make_site_goldens(args.out, meta, args.site)
     if args.only == "sites":
         return
+    make_stats_goldens(args.out, meta)
 
     rng = np.random.default_rng(20260101)
     day = 365.25

@@ -41,3 +41,15 @@ def test_decile_table_logic():
     for p, v, a, acres in rows:
         i = int(np.argmax(pr <= p))
         assert v == pr[i] and a == area[i] and np.isclose(acres, area[i] / 4046.86)
+
+
+def test_summary_statistics_matches_reference_text():
+    """utilities.summary_statistics reproduces the reference's table text on
+    the retained observations of its site files and on a table with NaNs."""
+    from onekapy_gb300.utilities import summary_statistics
+    d = golden("summary_statistics.npz")
+    for i in range(int(d["ncases"])):
+        vals = [tuple(r) for r in d[f"values_{i}"]]
+        got = summary_statistics(vals, list(d[f"names_{i}"]), list(d[f"formats_{i}"]),
+                                 str(d[f"title_{i}"])).getvalue()
+        assert got == str(d[f"text_{i}"]), i
