@@ -186,6 +186,16 @@ __device__ __forceinline__ bool in_umbra64(double bax, double bay, double cax, d
 // ProbabilityField.insert (probabilityfield.py:296-310) into a realization
 // bitmask: every node of the frame within umbra of segment a-b is OR-ed in,
 // one atomicOr per touched 32-node word of a row.
+// The reference's node test from the node's indices (the exact path of
+// insert64's FP32 pre-test).  Kept out of line so that the compiler cannot
+// evaluate it speculatively for every node: it runs for about 1 node in 5,000.
+static __device__ __noinline__ bool in_umbra64_node(double fxmin, int j, double dx, double ax, double bax, double bay,
+                                             double cay, double length2, double inv, bool fast_ok, double u2) {
+    const double cx = fxmin + (double)j * dx;
+    const double cax = cx - ax;
+    return in_umbra64(bax, bay, cax, cay, length2, inv, fast_ok, u2);
+}
+
 __device__ __forceinline__ void insert64(const Chron& ch, int gnrows, int gncols,
                                          const OnekaFrame& f, double dx, double dy, double umbra,
                                          double ax, double ay, double bx, double by,
@@ -204,19 +214,66 @@ __device__ __forceinline__ void insert64(const Chron& ch, int gnrows, int gncols
     const double length2 = bax * bax + bay * bay;
     const double inv = 1.0 / length2;
     const bool fast_ok = (length2 > 1e-250) && (inv < 1e250);
+    // FP32 pre-test.  The distance^2 of each node is first evaluated in FP32
+    // (cancellation-free form); a node whose FP32 value lies farther than
+    // `mf` from umbra^2 is decided by it, the others by the reference's FP64
+    // formula.  S bounds every coordinate magnitude of the node box
+    // (|cax| <= |bax| + umbra + dx, |cay| <= |bay| + umbra + dy), so each FP32
+    // operation errs by at most 2^-24 S^2 in the squared terms; the margin
+    // (256 + 4 k) 2^-24 S^2 covers them, the conversions, the k-node row
+    // offset and the reference's own FP64 rounding many times over.  The
+    // decisions, hence the counts, are the FP64 formula's.
+    const bool f32_ok = (length2 > 1e-20) && (length2 < 1e20) && (right - left) < (1 << 20);
+    float bxf = 0.0f, byf = 0.0f, l2f = 0.0f, u2f = 0.0f, dxf = 0.0f, mf = 0.0f;
+    if (f32_ok) {
+        bxf = (float)bax;
+        byf = (float)bay;
+        l2f = bxf * bxf + byf * byf;
+        u2f = (float)u2;
+        dxf = (float)dx;
+        const double S = 2.0 * (fabs(bax) + fabs(bay)) + 2.0 * umbra + dx + dy;
+        mf = (float)((256.0 + 4.0 * (right - left)) * 5.9604644775390625e-08 * S * S);
+    }
     for (int i = bottom; i < top; ++i) {
         const int gi = i + f.roff;
         if (gi < 0 || gi >= gnrows) continue;
         const double cy = f.ymin + (double)i * dy;
         const double cay = cy - ay;
+        float cayf = 0.0f, cax0f = 0.0f;
+        if (f32_ok) {
+            cayf = (float)cay;
+            cax0f = (float)((f.xmin + (double)left * dx) - ax);
+        }
         uint32_t acc = 0;
         int curw = -1;
         for (int j = left; j < right; ++j) {
             const int gj = j + f.coff;
             if (gj < 0 || gj >= gncols) continue;
-            const double cx = f.xmin + (double)j * dx;
-            const double cax = cx - ax;
-            if (in_umbra64(bax, bay, cax, cay, length2, inv, fast_ok, u2)) {
+            int decided = 0;                    // 1: inside, -1: outside, 0: FP64
+            if (f32_ok) {
+                // j - left as a float without the (FP64-pipe) I2F: exact below 2^22
+                const float kf = __int_as_float(0x4B400000 + (j - left)) - 12582912.0f;
+                const float caxf = fmaf(kf, dxf, cax0f);
+                const float dot = bxf * caxf + byf * cayf;
+                float d2;
+                if (dot < 0.0f) {
+                    d2 = caxf * caxf + cayf * cayf;
+                } else if (dot > l2f) {
+                    const float ex = caxf - bxf, ey = cayf - byf;
+                    d2 = ex * ex + ey * ey;
+                } else {
+                    const float p = bxf * cayf - byf * caxf;
+                    d2 = p * p / l2f;
+                }
+                if (d2 < u2f - mf) decided = 1;
+                else if (d2 > u2f + mf) decided = -1;
+            }
+            bool inside;
+            if (__builtin_expect(decided != 0, 1))
+                inside = decided > 0;
+            else
+                inside = in_umbra64_node(f.xmin, j, dx, ax, bax, bay, cay, length2, inv, fast_ok, u2);
+            if (inside) {
                 const int w = gj >> 5;
                 if (w != curw) {
                     if (acc) { ch.orw(gi, curw, acc); ++natom; }
