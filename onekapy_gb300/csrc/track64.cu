@@ -90,8 +90,8 @@ struct VertexSink {
 };
 
 template <bool CONFINED>
-__device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, const double* wx,
-                                        const double* wy, const double* wq, const Chron& ch);
+__device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, bool live,
+                                        const double* wx, const double* wy, const double* wq, const Chron& ch);
 
 template <bool CONFINED>
 __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
@@ -114,20 +114,27 @@ __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
     const long long idx = (long long)r * L.npaths + p;
     const bool skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
     if (!skip && blockIdx.x == 0 && threadIdx.x == 0 && L.registered) atomicAdd(L.registered, 1ull);
-    if (p < L.npaths) {
-        if (skip) {
-            if (L.out.status) L.out.status[idx] = kTraceSkipped;
-        } else {
-            trace64<CONFINED>(L, r, p, idx, wx, wy, wq, ch);
-        }
-    }
+    if (p < L.npaths && skip && L.out.status) L.out.status[idx] = kTraceSkipped;
+    // Every lane enters: the step loop is warp-uniform (see trace64).
+    trace64<CONFINED>(L, r, p, idx, p < L.npaths && !skip, wx, wy, wq, ch);
     __syncthreads();
     window_flush(ch);
 }
 
+// One particle per lane.  `live` is false for the lanes past npaths and for a
+// realization that is not tracked; such a lane reads and writes nothing but
+// still takes part in the warp's loop.
+//
+// The step loop is warp-uniform: it runs until every lane of the warp is done
+// (a __any_sync vote at the top), and lanes that are done sit out the body.
+// Only the chronicle insertion of an accepted step diverges, and the vote
+// brings the lanes back together before the next attempt, so the seven
+// stage evaluations issue once per warp rather than once per group of lanes
+// that happened to split apart in a variable-length insertion.  Each lane's
+// arithmetic is unchanged.
 template <bool CONFINED>
-__device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, const double* wx,
-                                        const double* wy, const double* wq, const Chron& ch) {
+__device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, bool live,
+                                        const double* wx, const double* wy, const double* wq, const Chron& ch) {
 
     Model64 m;
     m.wx = wx;
@@ -142,7 +149,8 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
     m.n = L.aquifer[3LL * r + 1];
     m.H = L.aquifer[3LL * r + 2];
 
-    const OnekaFrame f = frame_of(L, r, p);
+    OnekaFrame f = {};
+    if (live) f = frame_of(L, r, p);
     uint32_t* slot = ch.slot;
 
     const double dur = L.opts.duration;
@@ -150,11 +158,14 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
     const double maxstep = L.opts.maxstep;
     double t = 0.0;
     double dt = 0.1 * (dur > 0.0 ? 1.0 : (dur < 0.0 ? -1.0 : 0.0));
-    double x = L.release[2 * p];
-    double y = L.release[2 * p + 1];
+    double x = 0.0, y = 0.0;
+    if (live) {
+        x = L.release[2 * p];
+        y = L.release[2 * p + 1];
+    }
 
     VertexSink vs;
-    vs.v = L.out.vertices ? L.out.vertices + idx * 2LL * L.out.max_vertices : nullptr;
+    vs.v = (live && L.out.vertices) ? L.out.vertices + idx * 2LL * L.out.max_vertices : nullptr;
     vs.maxv = L.out.max_vertices;
     vs.n = 0;
     vs.push(x, y);
@@ -163,13 +174,23 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
     int acc = 0, att = 0;
     long long ntest = 0, natom = 0;
     int rlo = 0x7fffffff, rhi = -1;
-    double k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y, k5x, k5y, k6x, k6y, k7x, k7y;
-    if (!feval64<CONFINED>(m, x, y, k1x, k1y)) {
+    double k1x = 0.0, k1y = 0.0, k2x, k2y, k3x, k3y, k4x, k4y, k5x, k5y, k6x, k6y, k7x = 0.0, k7y = 0.0;
+    bool done = !live;
+    if (live && !feval64<CONFINED>(m, x, y, k1x, k1y)) {
         status = ONEKA_TRACE_DRY;
-    } else {
-        while (fabs(t) < fabs(dur)) {
+        done = true;
+    }
+    while (__any_sync(0xffffffffu, !done)) {
+        bool accept = false;
+        double xn = x, yn = y;
+        if (!done) do {
+            if (!(fabs(t) < fabs(dur))) {
+                done = true;
+                break;
+            }
             if (att >= L.max_attempts) {
                 status = ONEKA_TRACE_STEP_LIMIT;
+                done = true;
                 break;
             }
             ++att;
@@ -177,24 +198,22 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
             double px, py;
             px = x + dt * (DP::a2 * k1x);
             py = y + dt * (DP::a2 * k1y);
-            if (!feval64<CONFINED>(m, px, py, k2x, k2y)) { status = ONEKA_TRACE_DRY; break; }
+            if (!feval64<CONFINED>(m, px, py, k2x, k2y)) { status = ONEKA_TRACE_DRY; done = true; break; }
             px = x + dt * (DP::a31 * k1x + DP::a32 * k2x);
             py = y + dt * (DP::a31 * k1y + DP::a32 * k2y);
-            if (!feval64<CONFINED>(m, px, py, k3x, k3y)) { status = ONEKA_TRACE_DRY; break; }
+            if (!feval64<CONFINED>(m, px, py, k3x, k3y)) { status = ONEKA_TRACE_DRY; done = true; break; }
             px = x + dt * (DP::a41 * k1x + DP::a42 * k2x + DP::a43 * k3x);
             py = y + dt * (DP::a41 * k1y + DP::a42 * k2y + DP::a43 * k3y);
-            if (!feval64<CONFINED>(m, px, py, k4x, k4y)) { status = ONEKA_TRACE_DRY; break; }
+            if (!feval64<CONFINED>(m, px, py, k4x, k4y)) { status = ONEKA_TRACE_DRY; done = true; break; }
             px = x + dt * (DP::a51 * k1x + DP::a52 * k2x + DP::a53 * k3x + DP::a54 * k4x);
             py = y + dt * (DP::a51 * k1y + DP::a52 * k2y + DP::a53 * k3y + DP::a54 * k4y);
-            if (!feval64<CONFINED>(m, px, py, k5x, k5y)) { status = ONEKA_TRACE_DRY; break; }
+            if (!feval64<CONFINED>(m, px, py, k5x, k5y)) { status = ONEKA_TRACE_DRY; done = true; break; }
             px = x + dt * (DP::a61 * k1x + DP::a62 * k2x + DP::a63 * k3x + DP::a64 * k4x + DP::a65 * k5x);
             py = y + dt * (DP::a61 * k1y + DP::a62 * k2y + DP::a63 * k3y + DP::a64 * k4y + DP::a65 * k5y);
-            if (!feval64<CONFINED>(m, px, py, k6x, k6y)) { status = ONEKA_TRACE_DRY; break; }
-            const double xn = x + dt * (DP::a71 * k1x + DP::a73 * k3x + DP::a74 * k4x + DP::a75 * k5x +
-                                        DP::a76 * k6x);
-            const double yn = y + dt * (DP::a71 * k1y + DP::a73 * k3y + DP::a74 * k4y + DP::a75 * k5y +
-                                        DP::a76 * k6y);
-            if (!feval64<CONFINED>(m, xn, yn, k7x, k7y)) { status = ONEKA_TRACE_DRY; break; }
+            if (!feval64<CONFINED>(m, px, py, k6x, k6y)) { status = ONEKA_TRACE_DRY; done = true; break; }
+            xn = x + dt * (DP::a71 * k1x + DP::a73 * k3x + DP::a74 * k4x + DP::a75 * k5x + DP::a76 * k6x);
+            yn = y + dt * (DP::a71 * k1y + DP::a73 * k3y + DP::a74 * k4y + DP::a75 * k5y + DP::a76 * k6y);
+            if (!feval64<CONFINED>(m, xn, yn, k7x, k7y)) { status = ONEKA_TRACE_DRY; done = true; break; }
             const double ex = dt * (DP::e1 * k1x + DP::e2 * k7x + DP::e3 * k3x + DP::e4 * k4x +
                                     DP::e5 * k5x + DP::e6 * k6x);
             const double ey = dt * (DP::e1 * k1y + DP::e2 * k7y + DP::e3 * k3y + DP::e4 * k4y +
@@ -203,18 +222,8 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
             const double est = (isnan(aex) || isnan(aey)) ? (double)NAN : (aey > aex ? aey : aex);
             const double d0 = xn - x, d1 = yn - y;
             const double ds = sqrt(fma(d1, d1, d0 * d0));   // numpy.linalg.norm (OpenBLAS ddot)
-            if ((est < tol) && (ds < maxstep)) {
-                t = t + dt;
-                if (slot)
-                    insert64(ch, L.grid.nrows, L.grid.ncols, f, L.grid.dx, L.grid.dy,
-                             L.opts.umbra, x, y, xn, yn, ntest, natom, rlo, rhi);
-                k1x = k7x;
-                k1y = k7y;
-                x = xn;
-                y = yn;
-                vs.push(x, y);
-                ++acc;
-            }
+            accept = (est < tol) && (ds < maxstep);
+            if (accept) t = t + dt;
             // dt = 0.9 * min((tol/(est+EPS))**(1/5), maxstep/(ds+EPS), 10) * dt  (:247)
             const double fstep = maxstep / (ds + DP::eps);
             const double xq = tol / (est + DP::eps);
@@ -229,8 +238,20 @@ __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long
                 if (10.0 < fac) fac = 10.0;
             }
             dt = 0.9 * fac * dt;
+        } while (0);
+        if (accept) {
+            if (slot)
+                insert64(ch, L.grid.nrows, L.grid.ncols, f, L.grid.dx, L.grid.dy, L.opts.umbra, x, y, xn, yn,
+                         ntest, natom, rlo, rhi);
+            k1x = k7x;
+            k1y = k7y;
+            x = xn;
+            y = yn;
+            vs.push(x, y);
+            ++acc;
         }
     }
+    if (!live) return;
     if (L.out.endpoint) {
         L.out.endpoint[2 * idx] = x;
         L.out.endpoint[2 * idx + 1] = y;
