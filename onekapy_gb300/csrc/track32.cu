@@ -589,7 +589,11 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
             s.p = atomicAdd(&rc.next, 1);
         }
     }
-    while (live) {
+    // Warp-uniform: the vote gathers the lanes again before every attempt, so
+    // a divergent chronicle insertion or refill never leaves the warp running
+    // the next stage evaluations in separate groups.  BLOCK is a multiple of 32.
+    while (__any_sync(0xffffffffu, live)) {
+        if (!live) continue;
         live = attempt32<MODE, BLOCK>(L, rc, w, ch, s, r, cold);
         while (!live && s.p < pend) {
             finish32<BLOCK>(L, r, s, cold, ch);
