@@ -53,6 +53,7 @@ sys.path.insert(0, ROOT)
 METRIC = "realizations/s & particle-steps/s on 1 GB300 vs plain FP64; L∞ capture-prob err"
 UNIT = "realizations/s"
 SEED = 20261203
+TUNE_SAMPLE = 2048      # realizations the autotuner times each launch shape on (several waves)
 # DRAM bytes per realization of the tracking launch on this site, from one ncu
 # capture of a 1,000-realization launch (15.48 MB; profiles/).
 TRACK32_DRAM_BYTES_PER_REALIZATION = 15.48e6 / 1000
@@ -243,7 +244,7 @@ def run_ours(a):
     stream = torch.cuda.current_stream()
     # block shape / occupancy / chronicle window picked on a sample (setup, untimed)
     E.realize(site, R, seed=SEED, first=first, out=real)
-    o32 = E.autotune(site, real, release, o32, grid, sample=min(R, 1024))
+    o32 = E.autotune(site, real, release, o32, grid, sample=min(R, TUNE_SAMPLE))
 
     def step(opts, n, ev=None, outputs=None):
         counts.zero_()
@@ -374,7 +375,7 @@ def run_ours(a):
                 "e2e": {"value": e2e_n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "tracker_launch": {"block": o32.block, "occupancy": o32.occupancy,
-                                   "window_kb": o32.window_kb, "chosen_by": "autotune on 1024 realizations"},
+                                   "window_kb": o32.window_kb, "chosen_by": f"autotune on {min(R, TUNE_SAMPLE)} realizations"},
                 "gpu_launches": 3 * a.steps,
                 "clocks": clocks,
                 "cpu_baseline": cpu}
