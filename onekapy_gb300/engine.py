@@ -389,6 +389,21 @@ TUNE_CANDIDATES = [(256, 2, 32), (256, 3, 32), (128, 4, 32), (128, 6, 16), (128,
 _tuned: dict = {}
 
 
+def pick_fastest(n: int, time_one, repeats: int) -> tuple[int, list]:
+    """Index of the fastest of `n` candidates and each one's best time.
+    `time_one(i)` runs candidate i once and returns its duration.  The
+    candidates take turns: round 0 runs each once untimed (warm-up), then
+    `repeats` timed rounds run each once again, so a drift of the clock
+    during the tuning affects every candidate alike."""
+    best = [float("inf")] * n
+    for rnd in range(repeats + 1):
+        for i in range(n):
+            t = time_one(i)
+            if rnd > 0:
+                best[i] = min(best[i], t)
+    return min(range(n), key=lambda i: best[i]), best
+
+
 def site_signature(site: Site, grid: Grid, opts: TrackOptions, npaths: int) -> tuple:
     return (site.nwells, bool(opts.confined), int(opts.precision), grid.nrows, grid.ncols, int(npaths))
 
@@ -411,17 +426,16 @@ def autotune(site: Site, real: Realizations, release, opts: TrackOptions, grid: 
     scratch = scratch_buffer(grid.slot_bytes() * n, site.device)
     trials = [TrackOptions(**{**opts.__dict__, "block": b, "occupancy": o, "window_kb": w})
               for (b, o, w) in candidates]
-    best_times = [float("inf")] * len(trials)
-    for rnd in range(repeats + 1):
-        for i, trial in enumerate(trials):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            track(site, sub, release, trial, grid, counts=counts, scratch=scratch)
-            e1.record()
-            torch.cuda.synchronize()
-            if rnd > 0:
-                best_times[i] = min(best_times[i], e0.elapsed_time(e1))
-    i_best = min(range(len(trials)), key=lambda i: best_times[i])
+
+    def time_one(i):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        track(site, sub, release, trials[i], grid, counts=counts, scratch=scratch)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    i_best, best_times = pick_fastest(len(trials), time_one, repeats)
     if verbose:
         for (b, o, w), t in zip(candidates, best_times):
             print(f"autotune block={b} occupancy={o} window_kb={w}: {t:.3f} ms")

@@ -133,3 +133,23 @@ def test_synthetic_sites_have_the_configured_shapes():
     assert len(c3) == 64
     assert all(2 <= len(s.wells) - 1 <= 200 and 20 <= len(s.observations) <= 200 for s in c3)
     assert S.config1().observations == c1.observations   # seeded
+
+
+def test_autotune_candidates_take_turns():
+    """The launch-shape pick when the GPU speeds up by 5 % halfway through
+    the tuning.  Timed one after another, the later candidates would look
+    5 % faster and (9.2 * 0.95 < 9.0) the wrong shape would win; taking turns
+    gives every candidate timed runs after the change, so the best times
+    keep their true order."""
+    from onekapy_gb300 import engine as E
+    true_ms = [10.0, 9.0, 9.5, 9.2, 9.4, 9.3]          # candidate 1 is the fastest
+    calls = []
+
+    def time_one(i):
+        calls.append(i)
+        return true_ms[i] * (0.95 if len(calls) > 12 else 1.0)
+
+    best, times = E.pick_fastest(len(true_ms), time_one, repeats=3)
+    assert best == 1
+    assert calls == list(range(6)) * 4                  # one untimed round, then three timed
+    assert times == [t * 0.95 for t in true_ms]
