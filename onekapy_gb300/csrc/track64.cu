@@ -128,10 +128,10 @@ __global__ void __launch_bounds__(128) track64_kernel(const TrackLaunch L) {
 // The step loop is warp-uniform: it runs until every lane of the warp is done
 // (a __any_sync vote at the top), and lanes that are done sit out the body.
 // Only the chronicle insertion of an accepted step diverges, and the vote
-// brings the lanes back together before the next attempt, so the seven
-// stage evaluations issue once per warp rather than once per group of lanes
-// that happened to split apart in a variable-length insertion.  Each lane's
-// arithmetic is unchanged.
+// brings the lanes back together before the next attempt, so the six stage
+// evaluations (k2..k7) issue once per warp rather than once per group of
+// lanes that happened to split apart in a variable-length insertion.  Each
+// lane's arithmetic is unchanged.
 template <bool CONFINED>
 __device__ __forceinline__ void trace64(const TrackLaunch& L, int r, int p, long long idx, bool live,
                                         const double* wx, const double* wy, const double* wq, const Chron& ch) {
