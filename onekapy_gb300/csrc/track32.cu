@@ -145,7 +145,14 @@ __device__ __forceinline__ int floor_small(float x) {
     return (__float_as_int(b) - kMagicBits) - (r > x ? 1 : 0);
 }
 
-__device__ __forceinline__ int ceil_small(float x) { return -floor_small(-x); }
+// floor / ceil of a finite x already known to lie within +-2^22 (no clamp).
+__device__ __forceinline__ int floor_bounded(float x) {
+    const float b = __fadd_rn(x, kMagic);
+    const float r = __fsub_rn(b, kMagic);
+    return (__float_as_int(b) - kMagicBits) - (r > x ? 1 : 0);
+}
+
+__device__ __forceinline__ int ceil_bounded(float x) { return -floor_bounded(-x); }
 
 // clip_range for integer bounds [lo, hi) of a range of n nodes.
 __device__ __forceinline__ bool clip_int(int lo, int hi, int n, int& ilo, int& ihi) {
@@ -224,11 +231,18 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     const float k = BAX * iby, ae = fabsf(UL * iby);
     const float m = BAY * ibx, f = L2 * ibx;
     const float flo = fminf(0.0f, f), fhi = fmaxf(0.0f, f);
-    const float xlo = i2f_small(left) - 1.0f, xhi = i2f_small(right);
-    float t = i2f_small(bottom) * g.ryy - aY;       // row offset from a (units of dx)
-    for (int i = bottom; i < top; ++i, t += g.ryy) {
+    // Frame rows and columns that are grid nodes (gi = i + roff in [0, gnrows),
+    // gj = j + coff in [0, gncols)), clamped once for the segment: the row
+    // loop then needs no per-row range test, and clamping the interval to
+    // [cl - 1, cr] yields exactly the node span that clamping it to
+    // [left - 1, right] and then to the grid would.
+    const int rb = max(bottom, -roff), re = min(top, gnrows - roff);
+    const int cl = max(left, -coff), cr = min(right, gncols - coff);
+    if (rb >= re || cl >= cr) return;
+    const float xlo = i2f_small(cl) - 1.0f, xhi = i2f_small(cr);
+    float t = i2f_small(rb) * g.ryy - aY;           // row offset from a (units of dx)
+    for (int i = rb; i < re; ++i, t += g.ryy) {
         const int gi = i + roff;
-        if (gi < 0 || gi >= gnrows) continue;
         float LO = INFINITY, HI = -INFINITY;
         const float ha = g.U2 - t * t;
         if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
@@ -255,14 +269,12 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
         }
         if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
         if (!(LO < HI)) continue;
-        // nodes strictly inside (LO, HI), within the segment's columns [left, right)
-        const int jlo = floor_small(fmaxf(LO, xlo)) + 1;
-        const int jhi = ceil_small(fminf(HI, xhi)) - 1;
-        int glo = jlo + coff, ghi = jhi + coff;
-        glo = glo < 0 ? 0 : glo;
-        ghi = ghi >= gncols ? gncols - 1 : ghi;
-        if (glo > ghi) continue;
-        or_span(ch, gi, glo, ghi, natom);
+        // nodes strictly inside (LO, HI), within the columns [cl, cr); LO < HI
+        // here, so both clamped ends are finite and within [cl - 1, cr]
+        const int jlo = floor_bounded(fmaxf(LO, xlo)) + 1;
+        const int jhi = ceil_bounded(fminf(HI, xhi)) - 1;
+        if (jlo > jhi) continue;
+        or_span(ch, gi, jlo + coff, jhi + coff, natom);
         rlo = gi < rlo ? gi : rlo;
         rhi = gi > rhi ? gi : rhi;
     }
