@@ -26,6 +26,8 @@
 // sits in shared-memory columns, one per lane.
 #include <math.h>
 
+#include <type_traits>
+
 #include "oneka_internal.cuh"
 
 namespace oneka {
@@ -161,9 +163,25 @@ __device__ __forceinline__ bool clip_int(int lo, int hi, int n, int& ilo, int& i
     return ilo < ihi;
 }
 
-// OR the nodes gj in [glo, ghi] of grid row gi into the chronicle (the
-// row's window test is made once, not per word).
-__device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int ghi, long long& natom) {
+// OR the nodes gj in [glo, ghi] of grid row gi into the chronicle.  IN_WIN:
+// the caller has established that the whole span lies in the shared-memory
+// window, so no test is made.  Otherwise the row's window test is made once
+// and each word's once.
+template <bool IN_WIN>
+__device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int ghi, unsigned& natom) {
+    if (IN_WIN) {
+        const int base = (gi - ch.r0) * ch.nw - ch.w0;
+        int w = glo >> 5;
+        const int wl = ghi >> 5;
+        natom += wl - w + 1;
+        uint32_t m = 0xffffffffu << (glo & 31);
+        for (; w <= wl; ++w) {
+            if (w == wl) m &= 0xffffffffu >> (31 - (ghi & 31));
+            atomicOr(ch.win + (base + w), m);
+            m = 0xffffffffu;
+        }
+        return;
+    }
     const int ri = gi - ch.r0;
     const bool row_in = ch.win && (unsigned)ri < (unsigned)ch.nr;
     int w = glo >> 5;
@@ -203,8 +221,8 @@ struct Raster32 {
 // linear in it, with their order fixed per segment).
 __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols, int coff, int roff,
                                          int fncols, int fnrows, float fx0, float fy0, const Raster32& g,
-                                         float ax, float ay, float bx, float by, long long& ntest,
-                                         long long& natom, int& rlo, int& rhi) {
+                                         float ax, float ay, float bx, float by, unsigned& ntest,
+                                         unsigned& natom, int& rlo, int& rhi) {
     const float bax = bx - ax;
     const float bay = by - ay;
     if (!(bax * bax + bay * bay > 0.0f)) return;    // the reference's 0/0 marks nothing
@@ -215,7 +233,7 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     if (!clip_int(floor_small((fminf(ay, by) - g.umbra - fy0) * g.inv_dy),
                   floor_small((fmaxf(ay, by) + g.umbra - fy0) * g.inv_dy) + 1, fnrows, bottom, top))
         return;
-    ntest += (long long)(right - left) * (top - bottom);
+    ntest += (unsigned)(right - left) * (unsigned)(top - bottom);
     // segment in units of dx: X from column 0 of the frame, Y from row 0
     const float aX = (ax - fx0) * g.inv_dx, aY = (ay - fy0) * g.inv_dx;
     const float bX = (bx - fx0) * g.inv_dx, bY = (by - fy0) * g.inv_dx;
@@ -240,44 +258,55 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     const int cl = max(left, -coff), cr = min(right, gncols - coff);
     if (rb >= re || cl >= cr) return;
     const float xlo = i2f_small(cl) - 1.0f, xhi = i2f_small(cr);
-    float t = i2f_small(rb) * g.ryy - aY;           // row offset from a (units of dx)
-    for (int i = rb; i < re; ++i, t += g.ryy) {
-        const int gi = i + roff;
-        float LO = INFINITY, HI = -INFINITY;
-        const float ha = g.U2 - t * t;
-        if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
-        const float tb = t - BAY;
-        const float hb = g.U2 - tb * tb;
-        if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bX - h); HI = fmaxf(HI, bX + h); }
-        float slo, shi;
-        if (bay_nz) {
-            const float kt = k * t;
-            slo = kt - ae;
-            shi = kt + ae;
-        } else {
-            const bool in = fabsf(t) < g.U;
-            slo = in ? -INFINITY : INFINITY;
-            shi = in ? INFINITY : -INFINITY;
+    // The row loop, instantiated twice: for a node box that lies wholly in
+    // the shared-memory window (almost every segment near the target) the
+    // marks go there without per-row or per-word window tests.
+    auto rows = [&](auto in_win) {
+        float t = i2f_small(rb) * g.ryy - aY;           // row offset from a (units of dx)
+        for (int i = rb; i < re; ++i, t += g.ryy) {
+            const int gi = i + roff;
+            float LO = INFINITY, HI = -INFINITY;
+            const float ha = g.U2 - t * t;
+            if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
+            const float tb = t - BAY;
+            const float hb = g.U2 - tb * tb;
+            if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bX - h); HI = fmaxf(HI, bX + h); }
+            float slo, shi;
+            if (bay_nz) {
+                const float kt = k * t;
+                slo = kt - ae;
+                shi = kt + ae;
+            } else {
+                const bool in = fabsf(t) < g.U;
+                slo = in ? -INFINITY : INFINITY;
+                shi = in ? INFINITY : -INFINITY;
+            }
+            if (bax_nz) {
+                const float mt = -m * t;
+                slo = fmaxf(slo, mt + flo);
+                shi = fminf(shi, mt + fhi);
+            } else {
+                const float yc = BAY * t;
+                if (!(yc >= 0.0f && yc <= L2)) slo = INFINITY;
+            }
+            if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
+            if (!(LO < HI)) continue;
+            // nodes strictly inside (LO, HI), within the columns [cl, cr); LO < HI
+            // here, so both clamped ends are finite and within [cl - 1, cr]
+            const int jlo = floor_bounded(fmaxf(LO, xlo)) + 1;
+            const int jhi = ceil_bounded(fminf(HI, xhi)) - 1;
+            if (jlo > jhi) continue;
+            or_span<decltype(in_win)::value>(ch, gi, jlo + coff, jhi + coff, natom);
+            rlo = gi < rlo ? gi : rlo;
+            rhi = gi > rhi ? gi : rhi;
         }
-        if (bax_nz) {
-            const float mt = -m * t;
-            slo = fmaxf(slo, mt + flo);
-            shi = fminf(shi, mt + fhi);
-        } else {
-            const float yc = BAY * t;
-            if (!(yc >= 0.0f && yc <= L2)) slo = INFINITY;
-        }
-        if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
-        if (!(LO < HI)) continue;
-        // nodes strictly inside (LO, HI), within the columns [cl, cr); LO < HI
-        // here, so both clamped ends are finite and within [cl - 1, cr]
-        const int jlo = floor_bounded(fmaxf(LO, xlo)) + 1;
-        const int jhi = ceil_bounded(fminf(HI, xhi)) - 1;
-        if (jlo > jhi) continue;
-        or_span(ch, gi, jlo + coff, jhi + coff, natom);
-        rlo = gi < rlo ? gi : rlo;
-        rhi = gi > rhi ? gi : rhi;
-    }
+    };
+    const bool in_win = ch.win && rb + roff >= ch.r0 && re + roff <= ch.r0 + ch.nr &&
+                        ((cl + coff) >> 5) >= ch.w0 && ((cr - 1 + coff) >> 5) < ch.w0 + ch.nw;
+    if (in_win)
+        rows(std::true_type{});
+    else
+        rows(std::false_type{});
 }
 
 
@@ -509,7 +538,7 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
         s.yl = e;
         const float bxn = s.xh + s.xl, byn = s.yh + s.yl;
         if (ch.slot) {
-            long long ntest = (unsigned)c.i(kNtest), natom = (unsigned)c.i(kNatom);
+            unsigned ntest = (unsigned)c.i(kNtest), natom = (unsigned)c.i(kNatom);
             int rlo = c.i(kRlo), rhi = c.i(kRhi);
             insert32(ch, L.grid.nrows, L.grid.ncols, c.i(kCoff), c.i(kRoff), c.i(kNcols), c.i(kNrows),
                      c.f(kFx0), c.f(kFy0), rc.g, ax, ay,
