@@ -56,7 +56,7 @@ SEED = 20261203
 E2E_CALLS = 3           # timed public-API calls averaged into e2e
 TUNE_SAMPLE = 2048      # realizations the autotuner times each launch shape on (several waves)
 # DRAM bytes per realization of the tracking launch on this site, from one ncu
-# capture of a 1,000-realization launch (15.48 MB; profiles/).
+# capture of a 1,000-realization launch (15.48 MB).
 TRACK32_DRAM_BYTES_PER_REALIZATION = 15.48e6 / 1000
 
 
@@ -374,7 +374,7 @@ def run_ours(a):
                              "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
                              "traffic": TRACK32_DRAM_BYTES_PER_REALIZATION * R,
                              "traffic_source": "ncu dram__bytes_read+write of a 1000-realization launch, "
-                                               "scaled by realizations (profiles/track32_config2_1000real_full.md)",
+                                               "scaled by realizations",
                              "kernel": "track32_kernel (+ register_counts_kernel)",
                              "peak_source": "measured FP32 FMA loop on this GPU (oneka_fma_peak)"},
                 "roofline_hbm": _hbm_roofline(TRACK32_DRAM_BYTES_PER_REALIZATION * R, t_track),

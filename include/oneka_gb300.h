@@ -187,6 +187,29 @@ ONEKA_API int oneka_realize(const OnekaSite* site, const OnekaDist* qdist, const
                   const double* logr2, uint64_t seed, uint64_t first, int32_t nreal,
                   int32_t mode, OnekaRealizations* out, void* stream);
 
+/*
+ * Model.construct_fit (model.py:497-567) for one model on the device: the
+ * weighted rows WA [nobs][6] and right-hand side Wb [nobs] of the regional-
+ * flow least-squares problem, with the wells' discharges q [nwells] and the
+ * aquifer's conductivity and thickness, about the origin (site->xo, site->yo).
+ * FP64 in the reference's operation order.  *status (device int32) is set to
+ * ONEKA_REAL_OK, or ONEKA_REAL_RANGE where an observed head is at or below
+ * the base (the reference's RangeError; that row is NaN).
+ */
+ONEKA_API int oneka_fit_rows(const OnekaSite* site, const double* q, double conductivity, double thickness,
+                             double* WA, double* Wb, int32_t* status, void* stream);
+
+/*
+ * Model.compute_fit (model.py:571-606) for nfit independent problems:
+ * coef_ev [nfit][6], the least-squares solution of WA c = Wb (WA [nfit][nobs][6],
+ * Wb [nfit][nobs]), and coef_cov [nfit][36] = inv(WA^T WA), FP64 normal
+ * equations with a Jacobi-scaled Cholesky factor (one warp per problem).
+ * status [nfit] (may be NULL): ONEKA_REAL_OK, ONEKA_REAL_NOT_SPD (the
+ * reference's LinAlgError), or ONEKA_REAL_NOT_FINITE for a non-finite row.
+ */
+ONEKA_API int oneka_fit_solve(const double* WA, const double* Wb, int32_t nobs, int32_t nfit, double* coef_ev,
+                              double* coef_cov, int32_t* status, void* stream);
+
 /* Bytes of scratch oneka_track needs for `slots` realizations in flight. */
 ONEKA_API size_t oneka_track_scratch_bytes(const OnekaGrid* grid, int32_t slots);
 

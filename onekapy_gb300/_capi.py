@@ -29,7 +29,7 @@ EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_r
            "oneka_gaussian_filter", "oneka_count_histogram", "oneka_gemm_bf16", "oneka_bce_bitmask",
            "oneka_gelu_backward", "oneka_colsum_bf16", "oneka_adamw", "oneka_features",
            "oneka_sigmoid_colsum", "oneka_gemm_bf16_sigmoid_colsum", "oneka_gemm_bf16_path",
-           "oneka_gemm_tc_status"]
+           "oneka_gemm_tc_status", "oneka_fit_rows", "oneka_fit_solve"]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
@@ -108,6 +108,10 @@ def load() -> ctypes.CDLL:
         L.oneka_realize.argtypes = [ctypes.POINTER(OnekaSite), _P, ctypes.POINTER(OnekaDist), _P,
                                     ctypes.c_uint64, ctypes.c_uint64, _I, _I,
                                     ctypes.POINTER(OnekaRealizations), _P]
+        L.oneka_fit_rows.restype = ctypes.c_int
+        L.oneka_fit_rows.argtypes = [ctypes.POINTER(OnekaSite), _P, _D, _D, _P, _P, _P, _P]
+        L.oneka_fit_solve.restype = ctypes.c_int
+        L.oneka_fit_solve.argtypes = [_P, _P, _I, _I, _P, _P, _P, _P]
         L.oneka_track_scratch_bytes.restype = ctypes.c_size_t
         L.oneka_track_scratch_bytes.argtypes = [ctypes.POINTER(OnekaGrid), _I]
         L.oneka_track.restype = ctypes.c_int

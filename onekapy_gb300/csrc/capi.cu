@@ -16,6 +16,10 @@ cudaError_t launch_realize(const OnekaSite& site, const OnekaDist* qdist, const 
                            const double* logr2, unsigned long long seed, unsigned long long first,
                            int nreal, int mode, const OnekaRealizations& out, cudaStream_t s);
 cudaError_t launch_logr2(const OnekaSite& site, double* logr2, cudaStream_t s);
+cudaError_t launch_fit_rows(const OnekaSite& site, const double* q, double K, double H, double* WA, double* Wb,
+                            int32_t* status, cudaStream_t s);
+cudaError_t launch_fit_solve(const double* WA, const double* Wb, int nobs, int nfit, double* coef_ev,
+                             double* coef_cov, int32_t* status, cudaStream_t s);
 cudaError_t launch_register_weighted(uint32_t* mask, const OnekaGrid& g, double weight, double* pgrid,
                                      cudaStream_t s);
 cudaError_t launch_rasterize(const OnekaGrid& g, const OnekaFrame& f, const double* xy, long long n,
@@ -193,6 +197,27 @@ int oneka_realize(const OnekaSite* site, const OnekaDist* qdist, const OnekaDist
                         "adist kind");
     ONEKA_CHECK_CUDA(launch_realize(*site, qdist, adist, logr2, seed, first, nreal, mode, *out,
                                     (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_fit_rows(const OnekaSite* site, const double* q, double conductivity, double thickness, double* WA,
+                   double* Wb, int32_t* status, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(site && status, "site/status");
+    ONEKA_CHECK_ARG(site->nwells >= 0 && (site->nwells == 0 || (site->wells && q)), "wells/q");
+    ONEKA_CHECK_ARG(site->nobs >= 0 && (site->nobs == 0 || (site->obs && WA && Wb)), "observations/WA/Wb");
+    ONEKA_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), (cudaStream_t)stream));
+    ONEKA_CHECK_CUDA(launch_fit_rows(*site, q, conductivity, thickness, WA, Wb, status, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_fit_solve(const double* WA, const double* Wb, int32_t nobs, int32_t nfit, double* coef_ev,
+                    double* coef_cov, int32_t* status, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(nobs >= 0 && nfit >= 0, "nobs/nfit");
+    ONEKA_CHECK_ARG(nfit == 0 || (coef_ev && coef_cov), "coef_ev/coef_cov");
+    ONEKA_CHECK_ARG(nfit == 0 || nobs == 0 || (WA && Wb), "WA/Wb");
+    ONEKA_CHECK_CUDA(launch_fit_solve(WA, Wb, nobs, nfit, coef_ev, coef_cov, status, (cudaStream_t)stream));
     return ONEKA_OK;
 }
 

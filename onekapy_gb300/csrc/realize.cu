@@ -82,6 +82,131 @@ __device__ double variate_mean(const OnekaDist& d) {
     }
 }
 
+// One weighted row of the least-squares problem (model.py:545-565): the
+// FOSM potential of observation ob = (x, y, z_ev, z_std) under base, K, H,
+// less the wells' potential pw there, both over the potential's standard
+// deviation.  Returns false where the reference raises RangeError (a head at
+// or below the base).
+__device__ __forceinline__ bool fosm_row(const double* ob, double base, double K, double H, double xo,
+                                         double yo, double pw, double a[6], double& bo) {
+    const double x = ob[0], y = ob[1], z_ev = ob[2], z_std = ob[3];
+    const double head = z_ev - base;
+    double pot_ev, pot_std;
+    if (head >= H) {
+        pot_ev = (K * H * (head - 0.5 * H));
+        pot_std = K * H * z_std;
+    } else if (head > 0) {
+        pot_ev = (0.5 * K * (head * head + z_std * z_std));
+        pot_std = K * head * z_std;
+    } else {
+        return false;
+    }
+    const double dx = x - xo, dy = y - yo;
+    a[0] = dx * dx / pot_std;
+    a[1] = dy * dy / pot_std;
+    a[2] = dx * dy / pot_std;
+    a[3] = dx / pot_std;
+    a[4] = dy / pot_std;
+    a[5] = 1.0 / pot_std;
+    bo = (pot_ev - pw) / pot_std;
+    return true;
+}
+
+// N += a a^T (lower triangle, row by row), b += a bo.
+__device__ __forceinline__ void accumulate_normal(const double a[6], double bo, double N[21], double b[6]) {
+    int t = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+        for (int j = 0; j <= i; ++j) N[t++] += a[i] * a[j];
+        b[i] += a[i] * bo;
+    }
+}
+
+// Sum the lanes' normal equations (butterfly: every lane ends with the total).
+__device__ __forceinline__ void warp_reduce_normal(double N[21], double b[6], int& bad) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int i = 0; i < 21; ++i) N[i] += __shfl_xor_sync(0xffffffffu, N[i], off);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) b[i] += __shfl_xor_sync(0xffffffffu, b[i], off);
+        bad |= __shfl_xor_sync(0xffffffffu, bad, off);
+    }
+}
+
+// The least-squares solution and covariance from the normal equations
+// N c = b (model.py:597-604: lstsq(WA, Wb) and inv(WA^T WA)): Jacobi scaling
+// D = diag(N)^-1/2, Cholesky factor L of D N D, c = D L^-T L^-1 D b and
+// cov = D L^-T L^-1 D.  Returns ONEKA_REAL_OK or ONEKA_REAL_NOT_SPD (then ev
+// and cov are NaN).  L and d are kept for the MVN draw.
+__device__ int solve_normal(const double N[21], const double b[6], double L[6][6], double d[6], double ev[6],
+                            double cov[6][6]) {
+    int status = ONEKA_REAL_OK;
+    double A[6][6];
+    {
+        int t = 0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j <= i; ++j) { A[i][j] = N[t]; A[j][i] = N[t]; ++t; }
+    }
+    for (int i = 0; i < 6; ++i) {
+        ev[i] = 0.0;
+        if (!(A[i][i] > 0.0)) status = ONEKA_REAL_NOT_SPD;
+        d[i] = (A[i][i] > 0.0) ? 1.0 / sqrt(A[i][i]) : 0.0;
+    }
+    if (status == ONEKA_REAL_OK) {
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) A[i][j] *= d[i] * d[j];
+        for (int j = 0; j < 6 && status == ONEKA_REAL_OK; ++j) {
+            double s = A[j][j];
+            for (int k = 0; k < j; ++k) s -= L[j][k] * L[j][k];
+            if (!(s > 1e-14)) { status = ONEKA_REAL_NOT_SPD; break; }
+            L[j][j] = sqrt(s);
+            for (int i = j + 1; i < 6; ++i) {
+                double v = A[i][j];
+                for (int k = 0; k < j; ++k) v -= L[i][k] * L[j][k];
+                L[i][j] = v / L[j][j];
+            }
+            for (int i = 0; i < j; ++i) L[i][j] = 0.0;
+        }
+    }
+    if (status != ONEKA_REAL_OK) {
+        for (int i = 0; i < 6; ++i) {
+            ev[i] = NAN;
+            for (int j = 0; j < 6; ++j) cov[i][j] = NAN;
+        }
+        return status;
+    }
+    double y[6], z[6];
+    for (int i = 0; i < 6; ++i) {                 // L y = D b
+        double v = b[i] * d[i];
+        for (int k = 0; k < i; ++k) v -= L[i][k] * y[k];
+        y[i] = v / L[i][i];
+    }
+    for (int i = 5; i >= 0; --i) {                // L^T z = y
+        double v = y[i];
+        for (int k = i + 1; k < 6; ++k) v -= L[k][i] * z[k];
+        z[i] = v / L[i][i];
+    }
+    for (int i = 0; i < 6; ++i) ev[i] = d[i] * z[i];
+    // covariance (WA^T WA)^-1 = D L^-T L^-1 D
+    double Li[6][6];
+    for (int j = 0; j < 6; ++j) {
+        for (int i = 0; i < 6; ++i) {
+            double v = (i == j) ? 1.0 : 0.0;
+            for (int k = 0; k < i; ++k) v -= L[i][k] * Li[k][j];
+            Li[i][j] = (i < j) ? 0.0 : v / L[i][i];
+        }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double v = 0.0;
+            for (int k = (i > j ? i : j); k < 6; ++k) v += Li[k][i] * Li[k][j];
+            cov[i][j] = d[i] * d[j] * v;
+        }
+    return status;
+}
+
 struct RealizeParams {
     OnekaSite site;
     const OnekaDist* qdist;
@@ -144,112 +269,31 @@ __global__ void __launch_bounds__(32 * kWarps) realize_kernel(const RealizeParam
     int bad = 0;
     for (int o = lane; o < P.site.nobs; o += 32) {
         const double* ob = P.site.obs + 4LL * o;
-        const double x = ob[0], y = ob[1], z_ev = ob[2], z_std = ob[3];
-        const double head = z_ev - P.site.base;
-        double pot_ev, pot_std;
-        if (head >= H) {
-            pot_ev = (K * H * (head - 0.5 * H));
-            pot_std = K * H * z_std;
-        } else if (head > 0) {
-            pot_ev = (0.5 * K * (head * head + z_std * z_std));
-            pot_std = K * head * z_std;
-        } else {
-            bad = 1;
-            continue;
-        }
         double pw = 0.0;
         for (int w = 0; w < nw; ++w) {
             double l2;
             if (P.logr2) {
                 l2 = P.logr2[(long long)o * nw + w];
             } else {
-                const double ddx = x - P.site.wells[3 * w], ddy = y - P.site.wells[3 * w + 1];
+                const double ddx = ob[0] - P.site.wells[3 * w], ddy = ob[1] - P.site.wells[3 * w + 1];
                 l2 = log(ddx * ddx + ddy * ddy);
             }
             pw += q[w] * l2 * 0.07957747154594767;
         }
-        const double dx = x - P.site.xo, dy = y - P.site.yo;
-        double a[6] = {dx * dx / pot_std, dy * dy / pot_std, dx * dy / pot_std, dx / pot_std,
-                       dy / pot_std, 1.0 / pot_std};
-        const double bo = (pot_ev - pw) / pot_std;
-        int t = 0;
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-#pragma unroll
-            for (int j = 0; j <= i; ++j) N[t++] += a[i] * a[j];
-            b[i] += a[i] * bo;
+        double a[6], bo;
+        if (!fosm_row(ob, P.site.base, K, H, P.site.xo, P.site.yo, pw, a, bo)) {
+            bad = 1;
+            continue;
         }
+        accumulate_normal(a, bo, N, b);
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-        for (int i = 0; i < 21; ++i) N[i] += __shfl_xor_sync(0xffffffffu, N[i], off);
-#pragma unroll
-        for (int i = 0; i < 6; ++i) b[i] += __shfl_xor_sync(0xffffffffu, b[i], off);
-        bad |= __shfl_xor_sync(0xffffffffu, bad, off);
-    }
+    warp_reduce_normal(N, b, bad);
     if (lane != 0) return;
 
-    int status = bad ? ONEKA_REAL_RANGE : ONEKA_REAL_OK;
-    double A[6][6], L[6][6], d[6], ev[6] = {0, 0, 0, 0, 0, 0};
-    {
-        int t = 0;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j <= i; ++j) { A[i][j] = N[t]; A[j][i] = N[t]; ++t; }
-    }
-    if (status == ONEKA_REAL_OK) {
-        // (3) Jacobi scaling, Cholesky, solve (model.py:597-604)
-        for (int i = 0; i < 6; ++i) {
-            if (!(A[i][i] > 0.0)) status = ONEKA_REAL_NOT_SPD;
-            d[i] = (A[i][i] > 0.0) ? 1.0 / sqrt(A[i][i]) : 0.0;
-        }
-    }
-    if (status == ONEKA_REAL_OK) {
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) A[i][j] *= d[i] * d[j];
-        for (int j = 0; j < 6 && status == ONEKA_REAL_OK; ++j) {
-            double s = A[j][j];
-            for (int k = 0; k < j; ++k) s -= L[j][k] * L[j][k];
-            if (!(s > 1e-14)) { status = ONEKA_REAL_NOT_SPD; break; }
-            L[j][j] = sqrt(s);
-            for (int i = j + 1; i < 6; ++i) {
-                double v = A[i][j];
-                for (int k = 0; k < j; ++k) v -= L[i][k] * L[j][k];
-                L[i][j] = v / L[j][j];
-            }
-            for (int i = 0; i < j; ++i) L[i][j] = 0.0;
-        }
-    }
+    double L[6][6], d[6], ev[6], cov[6][6];
+    int status = bad ? ONEKA_REAL_RANGE : solve_normal(N, b, L, d, ev, cov);
     double coef[6] = {0, 0, 0, 0, 0, 0};
-    double cov[6][6];
     if (status == ONEKA_REAL_OK) {
-        double y[6], z[6];
-        for (int i = 0; i < 6; ++i) {                 // L y = D b
-            double v = b[i] * d[i];
-            for (int k = 0; k < i; ++k) v -= L[i][k] * y[k];
-            y[i] = v / L[i][i];
-        }
-        for (int i = 5; i >= 0; --i) {                // L^T z = y
-            double v = y[i];
-            for (int k = i + 1; k < 6; ++k) v -= L[k][i] * z[k];
-            z[i] = v / L[i][i];
-        }
-        for (int i = 0; i < 6; ++i) ev[i] = d[i] * z[i];
-        // covariance (WA^T WA)^-1 = D L^-T L^-1 D
-        double Li[6][6];
-        for (int j = 0; j < 6; ++j) {
-            for (int i = 0; i < 6; ++i) {
-                double v = (i == j) ? 1.0 : 0.0;
-                for (int k = 0; k < i; ++k) v -= L[i][k] * Li[k][j];
-                Li[i][j] = (i < j) ? 0.0 : v / L[i][i];
-            }
-        }
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
-                double v = 0.0;
-                for (int k = (i > j ? i : j); k < 6; ++k) v += Li[k][i] * Li[k][j];
-                cov[i][j] = d[i] * d[j] * v;
-            }
         // (4) multivariate-normal draw (stochastic.py:240-241): mean + D L^-T g
         if (draw_coef) {
             double g[6];
@@ -273,9 +317,10 @@ __global__ void __launch_bounds__(32 * kWarps) realize_kernel(const RealizeParam
         for (int i = 0; i < 6; ++i)
             if (!isfinite(ev[i]) || !isfinite(coef[i])) status = ONEKA_REAL_NOT_FINITE;
     } else {
-        for (int i = 0; i < 6; ++i)
+        for (int i = 0; i < 6; ++i) {
+            coef[i] = ev[i] = NAN;
             for (int j = 0; j < 6; ++j) cov[i][j] = NAN;
-        for (int i = 0; i < 6; ++i) { ev[i] = NAN; coef[i] = NAN; }
+        }
     }
     for (int i = 0; i < 6; ++i) P.out.coef[6LL * r + i] = coef[i];
     if (P.out.coef_ev)
@@ -286,6 +331,70 @@ __global__ void __launch_bounds__(32 * kWarps) realize_kernel(const RealizeParam
     if (!given)
         for (int a = 0; a < 3; ++a) P.out.aquifer[3LL * r + a] = aq[a];
     if (P.out.status) P.out.status[r] = status;
+}
+
+// construct_fit for one model (model.py:545-565): one thread per observation.
+__global__ void fit_rows_kernel(const OnekaSite site, const double* __restrict__ q, double K, double H,
+                                double* __restrict__ WA, double* __restrict__ Wb, int32_t* __restrict__ status) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= site.nobs) return;
+    const double* ob = site.obs + 4LL * o;
+    double pw = 0.0;                                   // compute_potential_wells_only (model.py:258-264)
+    for (int w = 0; w < site.nwells; ++w) {
+        const double ddx = ob[0] - site.wells[3 * w], ddy = ob[1] - site.wells[3 * w + 1];
+        pw += q[w] * log(ddx * ddx + ddy * ddy) * 0.07957747154594767;
+    }
+    double a[6], bo;
+    if (!fosm_row(ob, site.base, K, H, site.xo, site.yo, pw, a, bo)) {
+        for (int i = 0; i < 6; ++i) WA[6LL * o + i] = NAN;
+        Wb[o] = NAN;
+        atomicMax(status, ONEKA_REAL_RANGE);
+        return;
+    }
+    for (int i = 0; i < 6; ++i) WA[6LL * o + i] = a[i];
+    Wb[o] = bo;
+}
+
+// compute_fit (model.py:597-604) for nfit independent problems of nobs rows:
+// one warp per problem, lanes over the rows.
+__global__ void fit_solve_kernel(const double* __restrict__ WA, const double* __restrict__ Wb, int nobs,
+                                 int nfit, double* __restrict__ coef_ev, double* __restrict__ coef_cov,
+                                 int32_t* __restrict__ status) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f = blockIdx.x * kWarps + warp;
+    if (f >= nfit) return;
+    double N[21], b[6];
+#pragma unroll
+    for (int i = 0; i < 21; ++i) N[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) b[i] = 0.0;
+    int bad = 0;
+    for (int o = lane; o < nobs; o += 32) {
+        const double* row = WA + (6LL * nobs) * f + 6LL * o;
+        double a[6];
+        for (int i = 0; i < 6; ++i) a[i] = row[i];
+        const double bo = Wb[(long long)nobs * f + o];
+        bool fin = isfinite(bo);
+        for (int i = 0; i < 6; ++i) fin = fin && isfinite(a[i]);
+        if (!fin) {
+            bad = 1;
+            continue;
+        }
+        accumulate_normal(a, bo, N, b);
+    }
+    warp_reduce_normal(N, b, bad);
+    if (lane != 0) return;
+    double L[6][6], d[6], ev[6], cov[6][6];
+    int st = bad ? ONEKA_REAL_NOT_FINITE : solve_normal(N, b, L, d, ev, cov);
+    if (bad)
+        for (int i = 0; i < 6; ++i) {
+            ev[i] = NAN;
+            for (int j = 0; j < 6; ++j) cov[i][j] = NAN;
+        }
+    for (int i = 0; i < 6; ++i) coef_ev[6LL * f + i] = ev[i];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) coef_cov[36LL * f + 6 * i + j] = cov[i][j];
+    if (status) status[f] = st;
 }
 
 __global__ void logr2_kernel(OnekaSite site, double* __restrict__ logr2) {
@@ -316,6 +425,21 @@ cudaError_t launch_realize(const OnekaSite& site, const OnekaDist* qdist, const 
     const unsigned blocks = (unsigned)((nreal + kWarps - 1) / kWarps);
     const size_t smem = sizeof(double) * kWarps * (size_t)(site.nwells > 0 ? site.nwells : 1);
     realize_kernel<<<blocks, 32 * kWarps, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fit_rows(const OnekaSite& site, const double* q, double K, double H, double* WA, double* Wb,
+                            int32_t* status, cudaStream_t s) {
+    if (site.nobs <= 0) return cudaSuccess;
+    fit_rows_kernel<<<(unsigned)((site.nobs + 127) / 128), 128, 0, s>>>(site, q, K, H, WA, Wb, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fit_solve(const double* WA, const double* Wb, int nobs, int nfit, double* coef_ev,
+                             double* coef_cov, int32_t* status, cudaStream_t s) {
+    if (nfit <= 0) return cudaSuccess;
+    fit_solve_kernel<<<(unsigned)((nfit + kWarps - 1) / kWarps), 32 * kWarps, 0, s>>>(WA, Wb, nobs, nfit, coef_ev,
+                                                                                      coef_cov, status);
     return cudaGetLastError();
 }
 

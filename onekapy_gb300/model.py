@@ -139,51 +139,47 @@ class Model:
         return (coef_ev, coef_cov)
 
     def construct_fit(self, obs, xo, yo):
-        """WA, Wb of the weighted least-squares problem (model.py:497-567).  The
-        well potentials at the observations come from the GPU kernel."""
+        """WA, Wb of the weighted least-squares problem (model.py:497-567),
+        computed by the FP64 ``oneka_fit_rows`` kernel; host arrays
+        (nobs, 6) and (nobs, 1) as in the reference."""
         nobs = len(obs)
-        WA = np.zeros([nobs, 6])
-        Wb = np.zeros([nobs, 1])
         if nobs == 0:
-            return (WA, Wb)
-        pts = np.array([[o[0], o[1]] for o in obs], dtype=np.float64)
-        saved = self._coef
-        try:
-            self._coef = np.zeros(6)
-            pw = self.evaluate(pts)["potential"]
-        finally:
-            self._coef = saved
-        for i in range(nobs):
-            x, y, z_ev, z_std = obs[i]
-            head = z_ev - self.base
-            if head >= self.thickness:
-                pot_ev = (self.conductivity * self.thickness * (head - 0.5 * self.thickness))
-                pot_std = self.conductivity * self.thickness * z_std
-            elif head > 0:
-                pot_ev = (0.5 * self.conductivity * (head**2 + z_std**2))
-                pot_std = self.conductivity * head * z_std
-            else:
-                raise RangeError("model.fit_coeficient: elevation < base")
-            dx = x - xo
-            dy = y - yo
-            WA[i, :] = np.array([dx**2, dy**2, dx * dy, dx, dy, 1]) / pot_std
-            Wb[i] = (pot_ev - pw[i]) / pot_std
-        return (WA, Wb)
+            return (np.zeros([0, 6]), np.zeros([0, 1]))
+        dev = C.device()
+        site, wells, q = self._site(dev)
+        o = torch.as_tensor(np.asarray(obs, dtype=np.float64).reshape(-1, 4), device=dev).contiguous()
+        site.nobs, site.obs, site.xo, site.yo = nobs, C.ptr(o), float(xo), float(yo)
+        WA = torch.empty((nobs, 6), dtype=torch.float64, device=dev)
+        Wb = torch.empty((nobs, 1), dtype=torch.float64, device=dev)
+        st = torch.empty(1, dtype=torch.int32, device=dev)
+        C.check(C.load().oneka_fit_rows(ctypes.byref(site), C.ptr(q) if len(self.wells) else None,
+                                        float(self.conductivity), float(self.thickness), C.ptr(WA), C.ptr(Wb),
+                                        C.ptr(st), C.stream_ptr()))
+        if int(st.item()) == C.REAL_RANGE:
+            raise RangeError("model.fit_coeficient: elevation < base")
+        return (WA.cpu().numpy(), Wb.cpu().numpy())
 
     @staticmethod
     def compute_fit(WA, Wb):
-        """Least-squares coefficients and covariance (model.py:571-606), solved
-        on the GPU with cuSOLVER through torch.linalg."""
+        """Least-squares coefficients (6, 1) and covariance inv(WA^T WA) (6, 6)
+        (model.py:571-606), solved by the FP64 ``oneka_fit_solve`` kernel
+        (normal equations with a Jacobi-scaled Cholesky factor)."""
         dev = C.device()
-        A = torch.as_tensor(np.asarray(WA, dtype=np.float64), device=dev)
-        b = torch.as_tensor(np.asarray(Wb, dtype=np.float64).reshape(-1, 1), device=dev)
-        N = A.T @ A
-        try:
-            coef_ev = torch.linalg.lstsq(A, b).solution
-            coef_cov = torch.linalg.inv(N)
-        except RuntimeError as e:
-            raise np.linalg.LinAlgError(str(e))
-        return (coef_ev.cpu().numpy(), coef_cov.cpu().numpy())
+        A = torch.as_tensor(np.asarray(WA, dtype=np.float64).reshape(-1, 6), device=dev).contiguous()
+        b = torch.as_tensor(np.asarray(Wb, dtype=np.float64).reshape(-1), device=dev).contiguous()
+        if b.shape[0] != A.shape[0]:
+            raise ValueError("WA and Wb must have the same number of rows")
+        ev = torch.empty((1, 6), dtype=torch.float64, device=dev)
+        cov = torch.empty((1, 36), dtype=torch.float64, device=dev)
+        st = torch.empty(1, dtype=torch.int32, device=dev)
+        C.check(C.load().oneka_fit_solve(C.ptr(A), C.ptr(b), A.shape[0], 1, C.ptr(ev), C.ptr(cov), C.ptr(st),
+                                         C.stream_ptr()))
+        s = int(st.item())
+        if s == C.REAL_NOT_SPD:
+            raise np.linalg.LinAlgError("normal equations are not positive definite")
+        if s != C.REAL_OK:
+            raise np.linalg.LinAlgError("WA or Wb is not finite")
+        return (ev.cpu().numpy().reshape(6, 1), cov.cpu().numpy().reshape(6, 6))
 
 
 def fit(model: Model, obs, xo, yo):

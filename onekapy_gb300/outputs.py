@@ -25,13 +25,23 @@ class CaptureZoneError(Exception):
     """Empty capture zone (oneka/visualize.py:224-226)."""
 
 
+def _pgrid(pfield) -> torch.Tensor:
+    """The field's weighted counts as a device tensor (a field held on the
+    host, such as one loaded from an archive, is copied to the device)."""
+    dev = getattr(pfield, "pgrid_device", None)
+    if dev is not None:
+        return dev
+    return torch.as_tensor(np.asarray(pfield.pgrid, dtype=np.float64), device=C.device())
+
+
 def probability(pfield) -> torch.Tensor:
     """pgrid / total_weight as an IEEE division per cell, as NumPy computes it
     (a tensor divided by a Python scalar would be multiplied by the
     reciprocal instead, which differs in the last bit)."""
     if pfield.total_weight <= 0:
         raise CaptureZoneError("Empty capture zone")
-    return torch.div(pfield.pgrid, torch.full_like(pfield.pgrid, float(pfield.total_weight)))
+    pg = _pgrid(pfield)
+    return torch.div(pg, torch.full_like(pg, float(pfield.total_weight)))
 
 
 def gaussian_weights(sigma: float, truncate: float = 4.0) -> np.ndarray:
@@ -59,7 +69,7 @@ def _integer_counts(pfield):
     counts = getattr(pfield, "counts", None)
     if counts is not None:
         return counts
-    pg = pfield.pgrid
+    pg = _pgrid(pfield)
     if float(pfield.total_weight).is_integer() and bool((pg == torch.round(pg)).all()):
         return pg.to(torch.int32)
     return None
@@ -71,7 +81,7 @@ def impact_curve(spacing, pfield):
     if pfield.total_weight <= 0:
         raise CaptureZoneError("Empty capture zone")
     counts = _integer_counts(pfield)
-    n = int(pfield.pgrid.numel())
+    n = int(_pgrid(pfield).numel())
     if counts is not None and float(pfield.total_weight) == float(int(pfield.total_weight)):
         R = int(pfield.total_weight)
         nb = int(max(R, int(counts.max().item())) + 1)

@@ -1,11 +1,20 @@
 """Drop-in ``ProbabilityField`` of oneka/probabilityfield.py:53-427 with its
 grids on the GPU.
 
-``pgrid`` is a float64 device tensor [nrows, ncols]; the per-realization
-registration grid is a device bitmask (``ceil(ncols/32)`` uint32 words per
-row) that ``rgrid`` presents as a bool tensor.  ``insert`` / ``rasterize`` run
-the FP64 ``oneka_rasterize`` kernel, ``register`` the ``oneka_register_weighted``
-kernel; the geometry (expand) is host bookkeeping, as in the reference.
+The grids live on the device: ``pgrid_device`` is a float64 tensor
+[nrows, ncols] and the per-realization registration grid is a device bitmask
+(``ceil(ncols/32)`` uint32 words per row, ``mask``).  ``insert`` /
+``rasterize`` run the FP64 ``oneka_rasterize`` kernel, ``register`` the
+``oneka_register_weighted`` kernel; the geometry (expand) is host
+bookkeeping, as in the reference.
+
+``pgrid`` and ``rgrid`` are what the reference's callers read
+(``pf.pgrid/pf.total_weight`` and ``np.sort(...)`` in oneka/visualize.py:230,
+:318, :382): host NumPy arrays, float64 and bool, as in the reference.
+``pgrid`` is copied back from the device once per change of the device grid
+and cached; ``rgrid`` is unpacked from the bitmask on every read.  Writing an
+element of the returned arrays does not reach the device: assign a whole
+array (``pf.pgrid = a``, ``pf.rgrid = b``) instead.
 """
 from __future__ import annotations
 
@@ -55,7 +64,9 @@ class ProbabilityField:
         self.deltax = deltax
         self.deltay = deltay
         self._mask = None
-        self.pgrid = None
+        self._pdev = None        # device float64 [nrows, ncols]
+        self._phost = None       # cached host copy of _pdev (None: not copied yet)
+        self._rhost = None       # host rgrid of a field unpickled without a GPU
         if np.isnan(xo) or np.isnan(yo):
             self.nrows = 0
             self.ncols = 0
@@ -78,19 +89,49 @@ class ProbabilityField:
 
     def _alloc(self):
         dev = C.device()
-        self.pgrid = torch.zeros((self.nrows, self.ncols), dtype=torch.float64, device=dev)
+        self._pdev = torch.zeros((self.nrows, self.ncols), dtype=torch.float64, device=dev)
+        self._phost = None
         self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=dev)
 
     @property
-    def rgrid(self) -> torch.Tensor:
-        """The registration grid of the current realization as bool [nrows, ncols]."""
-        if self._mask is None and getattr(self, "_host_rgrid", None) is not None:
-            return self._host_rgrid
+    def pgrid(self) -> np.ndarray | None:
+        """The weighted counts as a host float64 array [nrows, ncols] (the
+        reference's type), copied from the device when it last changed."""
+        if self._pdev is None:
+            return self._phost
+        if self._phost is None:
+            self._phost = self._pdev.cpu().numpy()
+        return self._phost
+
+    @pgrid.setter
+    def pgrid(self, value):
+        if isinstance(value, torch.Tensor):
+            self._pdev = value.to(dtype=torch.float64, device=C.device())
+        else:
+            self._pdev = torch.as_tensor(np.asarray(value, dtype=np.float64), device=C.device())
+        self._phost = None
+
+    @property
+    def pgrid_device(self) -> torch.Tensor | None:
+        """The weighted counts on the device (float64 [nrows, ncols])."""
+        return self._pdev
+
+    @property
+    def rgrid_device(self) -> torch.Tensor:
+        """The registration grid of the current realization as a device bool tensor."""
         return _unpack(self._mask, self.nrows, self.ncols, (self.ncols + 31) // 32)
+
+    @property
+    def rgrid(self) -> np.ndarray:
+        """The registration grid of the current realization as a host bool array [nrows, ncols]."""
+        if self._mask is None:
+            return self._rhost
+        return self.rgrid_device.cpu().numpy()
 
     @rgrid.setter
     def rgrid(self, value):
-        v = torch.as_tensor(value, device=self._mask.device).to(torch.bool)
+        v = torch.as_tensor(np.asarray(value) if not isinstance(value, torch.Tensor) else value,
+                            device=self._mask.device).to(torch.bool)
         self._mask = _pack(v, (self.ncols + 31) // 32, self._mask_words())
 
     @property
@@ -147,13 +188,14 @@ class ProbabilityField:
             self._regrid(nrows, ncols, rshift, cshift)
 
     def _regrid(self, nrows, ncols, rshift, cshift):
-        old_r = self.rgrid
-        dev = self.pgrid.device
+        old_r = self.rgrid_device
+        dev = self._pdev.device
         pgrid = torch.zeros((nrows, ncols), dtype=torch.float64, device=dev)
-        pgrid[rshift:rshift + self.nrows, cshift:cshift + self.ncols] = self.pgrid
+        pgrid[rshift:rshift + self.nrows, cshift:cshift + self.ncols] = self._pdev
         rgrid = torch.zeros((nrows, ncols), dtype=torch.bool, device=dev)
         rgrid[rshift:rshift + self.nrows, cshift:cshift + self.ncols] = old_r
-        self.pgrid = pgrid
+        self._pdev = pgrid
+        self._phost = None
         self.nrows, self.ncols = nrows, ncols
         self._mask = _pack(rgrid, (ncols + 31) // 32, self._mask_words())
 
@@ -183,7 +225,8 @@ class ProbabilityField:
         self.total_weight += weight
         g = self._grid().c()
         C.check(C.load().oneka_register_weighted(ctypes.byref(g), C.ptr(self._mask), float(weight),
-                                                 C.ptr(self.pgrid), C.stream_ptr()))
+                                                 C.ptr(self._pdev), C.stream_ptr()))
+        self._phost = None
 
     def reset(self):
         """Clear rgrid (probabilityfield.py:362-376)."""
@@ -200,12 +243,14 @@ class ProbabilityField:
 
     # ---------------------------------------------------------------- pickling
     def __getstate__(self):
-        """Host arrays under the reference's attribute names (archive.py)."""
+        """The reference's attributes, with pgrid / rgrid as host NumPy arrays
+        (oneka/probabilityfield.py:125-151), so that the state is the one a
+        reference ProbabilityField pickles."""
         st = {k: v for k, v in self.__dict__.items()
-              if k not in ("_mask", "pgrid", "realizations", "counts", "_host_rgrid")}
+              if not k.startswith("_") and k not in ("realizations", "counts")}
         if self.nrows:
-            st["pgrid"] = self.pgrid.detach().cpu().numpy()
-            st["rgrid"] = self.rgrid.cpu().numpy()
+            st["pgrid"] = np.array(self.pgrid, dtype=np.float64)
+            st["rgrid"] = np.array(self.rgrid, dtype=bool)
         return st
 
     def __setstate__(self, st):
@@ -214,19 +259,22 @@ class ProbabilityField:
         rgrid = st.pop("rgrid", None)
         self.__dict__.update(st)
         self._mask = None
-        self.pgrid = None
-        self._host_rgrid = None
-        if pgrid is not None:
-            if torch.cuda.is_available():
-                dev = C.device()
-                self.pgrid = torch.as_tensor(pgrid, device=dev)
-                self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=dev)
-                self.rgrid = torch.as_tensor(rgrid, device=dev)
-            else:           # inspection without a GPU: host arrays
-                self.pgrid = torch.as_tensor(pgrid)
-                self._host_rgrid = torch.as_tensor(rgrid)
+        self._pdev = None
+        self._phost = None
+        self._rhost = None
+        if pgrid is None:
+            return
+        if torch.cuda.is_available():
+            self.pgrid = pgrid
+            self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=C.device())
+            self.rgrid = rgrid
+        else:           # inspection without a GPU: host arrays only
+            self._phost = np.asarray(pgrid, dtype=np.float64)
+            self._rhost = np.asarray(rgrid, dtype=bool)
 
     # ---------------------------------------------------------------- helpers
     def probability(self) -> torch.Tensor:
-        """pgrid / total_weight (the capture probability, oneka/visualize.py:230)."""
-        return self.pgrid / self.total_weight
+        """pgrid / total_weight on the device (the capture probability,
+        oneka/visualize.py:230)."""
+        from .outputs import probability
+        return probability(self)

@@ -5,7 +5,8 @@ in the development container, where the reference sources are mounted; the
 fixtures it writes travel with the repository, and the tests compare against
 them.  It never touches the product package.
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    ONEKA_REFERENCE=<path of the OnekaPy checkout> python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <path of the OnekaPy checkout>
 
 What it records (all FP64, as the reference computes):
 
@@ -32,6 +33,19 @@ reference's site files as inputs next to its outputs on them.
 
     python tests/golden/make_golden.py --only sites     # just the site fixtures
     python tests/golden/make_golden.py --only stats     # just summary_statistics.npz
+    python tests/golden/make_golden.py --only archive   # just archive_reference.bz2
+    python tests/golden/make_golden.py --only fitrows   # just fit_rows_cases.npz
+
+* ``fit_rows_cases.npz``: the reference's ``Model.construct_fit`` rows WA, Wb
+  and ``Model.compute_fit`` solution on the inputs of ``fit_cases.npz``.
+
+* ``archive_reference.bz2`` (+ ``archive_reference.npz``, the field it holds):
+  an archive written by the reference's own ``dump_oneka``
+  (oneka/archive.py:46-82) of a reference ProbabilityField with registered
+  weights and a pending registration grid.  The same run checks the other
+  direction: an archive written by ``onekapy_gb300.archive.dump_oneka`` is
+  opened by the reference's ``load_oneka`` (oneka/archive.py:85-89) and
+  yields the reference's class with the same attributes.
 """
 from __future__ import annotations
 
@@ -223,23 +237,97 @@ def run_track_case(M, C, PF, name, *, wells, obs, base, real, npaths, duration, 
     return out
 
 
+def make_archive_goldens(out, meta, PF):
+    """An archive written by the reference, and the check that the reference
+    reads one written by this package."""
+    import glob
+    import shutil
+    from oneka import archive as RA
+    pf = PF.ProbabilityField(10.0, 10.0, 0.0, 0.0)
+    rr = np.random.default_rng(5)
+    for k, w in enumerate([1.0, 1.0, 0.5, 2.0]):
+        pts = rr.uniform(-150, 150, size=2) + np.cumsum(rr.normal(0, 20, size=(12, 2)), axis=0)
+        pf.rasterize(list(pts[:, 0]), list(pts[:, 1]), 15.0)
+        pf.register(w)
+    pts = np.cumsum(rr.normal(0, 20, size=(6, 2)), axis=0)
+    pf.rasterize(list(pts[:, 0]), list(pts[:, 1]), 12.0)     # pending: rgrid set, not registered
+    args = ("archive-golden", 12.5, 0, 24, 3652.5, 4, 0.0, (5.0, 10.0), 0.25, (20.0, 25.0, 30.0),
+            [(0.0, 0.0, 0.25, (400.0, 600.0))], [(100.0, 50.0, 30.0, 0.1)], 100.0, 10.0, 15.0, 2.0,
+            True, 1.0, 10.0)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as td:
+        os.chdir(td)
+        try:
+            RA.dump_oneka(*args, pf)
+        finally:
+            os.chdir(cwd)
+        written = glob.glob(os.path.join(td, "*Oneka*.bz2")) + glob.glob(os.path.join(td, "logs", "Oneka*.bz2"))
+        assert len(written) == 1, written
+        shutil.copyfile(written[0], os.path.join(out, "archive_reference.bz2"))
+    np.savez_compressed(os.path.join(out, "archive_reference.npz"), pgrid=pf.pgrid, rgrid=pf.rgrid,
+                        geometry=np.array([pf.deltax, pf.deltay, pf.nrows, pf.ncols, pf.xmin, pf.xmax,
+                                           pf.ymin, pf.ymax, pf.total_weight]), **meta)
+    # the other direction: this package's archive, read by the reference
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from onekapy_gb300 import archive as OA
+    from onekapy_gb300.probabilityfield import ProbabilityField as OurPF
+    ours = OurPF.__new__(OurPF)
+    ours.__setstate__(dict(pf.__dict__))
+    with tempfile.TemporaryDirectory() as td:
+        fn = OA.dump_oneka(*args, ours, filename=os.path.join(td, "ours.bz2"))
+        d = RA.load_oneka(fn)
+    got = d["pfield"]
+    assert type(got) is PF.ProbabilityField, type(got)
+    for k in ("deltax", "deltay", "nrows", "ncols", "xmin", "xmax", "ymin", "ymax", "total_weight"):
+        assert getattr(got, k) == getattr(pf, k), k
+    assert got.pgrid.dtype == np.float64 and np.array_equal(got.pgrid, pf.pgrid)
+    assert got.rgrid.dtype == bool and np.array_equal(got.rgrid, pf.rgrid)
+    print("archive: reference archive written; this package's archive read by the reference's load_oneka")
+
+
+def make_fit_rows_goldens(out, meta, M):
+    """construct_fit (WA, Wb) and compute_fit (ev, cov) of the reference on the fit cases' inputs."""
+    d = np.load(os.path.join(out, "fit_cases.npz"))
+    rows = {}
+    for i in range(int(d["ncases"])):
+        wq = [tuple(float(v) for v in r) for r in d[f"wells_{i}"]]
+        ob = [tuple(float(v) for v in r) for r in d[f"obs_{i}"]]
+        mo = M.Model(float(d[f"base_{i}"]), float(d[f"K_{i}"]), 0.25, float(d[f"H_{i}"]), wq)
+        WA, Wb = mo.construct_fit(ob, wq[0][0], wq[0][1])
+        ev, cov = M.Model.compute_fit(WA, Wb)
+        rows.update({f"WA_{i}": WA, f"Wb_{i}": Wb, f"ev_{i}": ev, f"cov_{i}": cov, f"xo_{i}": wq[0][0],
+                     f"yo_{i}": wq[0][1]})
+    np.savez_compressed(os.path.join(out, "fit_rows_cases.npz"), ncases=int(d["ncases"]), **rows, **meta)
+    print("fit rows: construct_fit and compute_fit of", int(d["ncases"]), "cases")
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("ONEKA_REFERENCE"),
+                    help="OnekaPy checkout (default: $ONEKA_REFERENCE)")
     ap.add_argument("--out", default=HERE)
-    ap.add_argument("--only", choices=["sites", "stats"], default=None)
+    ap.add_argument("--only", choices=["sites", "stats", "archive", "fitrows"], default=None)
     ap.add_argument("--site", action="append", default=None, help="with --only sites: these site files only")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("give --reference or set ONEKA_REFERENCE to the OnekaPy checkout")
     M, C, PF = import_reference(args.reference)
     meta = dict(numpy=np.__version__, python=platform.python_version(), machine=platform.machine())
     print("reference imported;", meta)
     if args.only == "stats":
         make_stats_goldens(args.out, meta)
         return
+    if args.only == "archive":
+        make_archive_goldens(args.out, meta, PF)
+        return
+    if args.only == "fitrows":
+        make_fit_rows_goldens(args.out, meta, M)
+        return
     make_site_goldens(args.out, meta, args.site)
     if args.only == "sites":
         return
     make_stats_goldens(args.out, meta)
+    make_archive_goldens(args.out, meta, PF)
 
     rng = np.random.default_rng(20260101)
     day = 365.25
@@ -344,6 +432,7 @@ def main():
     np.savez_compressed(os.path.join(args.out, "fit_cases.npz"),
                         **{f"{k}_{i}": v for i, d in enumerate(fit_rows) for k, v in d.items()},
                         ncases=len(fit_rows), **meta)
+    make_fit_rows_goldens(args.out, meta, M)
 
     # ---- rasterize: random polylines on a fixed window (incl. zero-length and off-grid).
     rr = np.random.default_rng(7)

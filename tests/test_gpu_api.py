@@ -74,7 +74,7 @@ def test_compute_capturezone_dropin_on_growing_grid():
                             1.0, float(d["tol"]), float(d["maxstep"]), make_feval(mo, bool(d["confined"])))
     assert (pf.xmin, pf.ymin, pf.nrows, pf.ncols) == (d["grid"][0], d["grid"][1], d["grid"][4], d["grid"][5])
     assert pf.total_weight == d["total_weight"]
-    assert np.array_equal(pf.pgrid.cpu().numpy(), d["counts"].astype(np.float64))
+    assert np.array_equal(pf.pgrid, d["counts"].astype(np.float64))
 
 
 def test_config1_full_fp64_bit_exact_vs_oracle(oracle_mod):
@@ -151,7 +151,50 @@ def test_create_stochastic_capturezone_dropin(oracle_mod):
                             real.q.cpu().numpy(), real.aquifer.cpu().numpy(), site.release(24),
                             (xmin, ymin, 10.0, 10.0, nrows, ncols), duration=spec.duration, tol=1,
                             maxstep=10, umbra=20, confined=True, frames=frames, xo=site.xo, yo=site.yo)
-    assert np.array_equal(pf.pgrid.cpu().numpy(), want["counts"].astype(np.float64))
+    assert np.array_equal(pf.pgrid, want["counts"].astype(np.float64))
+
+
+def test_returned_field_runs_the_reference_callers_unchanged(oracle_mod):
+    """create_stochastic_capturezone returns a field on which the reference's
+    own caller code runs as written: Z = pf.pgrid/pf.total_weight
+    (oneka/visualize.py:230), the impact curve's sort (visualize.py:382-384)
+    and the decile loop (oneka/oneka.py:278-288); each gives the values that
+    the oracle's counts give."""
+    from onekapy_gb300.stochastic import create_stochastic_capturezone
+    spec = S.config1()
+    pf = create_stochastic_capturezone(0, 32, spec.duration, 10, spec.base, spec.c_dist, spec.p_dist,
+                                       spec.t_dist, spec.wells, spec.observations, spec.spacing, spec.umbra,
+                                       True, spec.tol, spec.maxstep, seed=21, window=spec.half)
+    site = _site(spec)
+    spec32 = S.config1()
+    spec32.npaths = 32
+    grid = E.Grid(pf.xmin, pf.ymin, pf.deltax, pf.deltay, pf.nrows, pf.ncols)
+    want = _oracle_counts(oracle_mod, site, pf.realizations, spec32, grid)["counts"].astype(np.float64)
+    assert isinstance(pf.pgrid, np.ndarray) and pf.pgrid.dtype == np.float64
+    assert isinstance(pf.rgrid, np.ndarray) and pf.rgrid.dtype == bool
+    spacing = spec.spacing
+    # oneka/visualize.py:230
+    Z = pf.pgrid/pf.total_weight
+    assert np.array_equal(Z, want / 10.0)
+    # oneka/visualize.py:382-384
+    pr = np.flip(np.sort(pf.pgrid/pf.total_weight, axis=None))
+    n = pr.shape[0]
+    area = (np.arange(n)+1)*spacing**2
+    pr_want = np.flip(np.sort(want / 10.0, axis=None))
+    assert np.array_equal(pr, pr_want)
+    # oneka/oneka.py:278-288
+    rows, rows_want = [], []
+    for p in np.linspace(0.05, 0.95, 19):
+        i = np.argmax(pr <= p)
+        rows.append('{0:8.3f} {1:16,.0f} {2:16,.2f}'.format(pr[i], area[i], area[i] / 4046.86))
+        j = np.argmax(pr_want <= p)
+        rows_want.append('{0:8.3f} {1:16,.0f} {2:16,.2f}'.format(pr_want[j], area[j], area[j] / 4046.86))
+    assert rows == rows_want
+    from onekapy_gb300.outputs import decile_table, impact_curve
+    pr2, area2 = impact_curve(spacing, pf)
+    assert np.array_equal(pr2, pr) and np.array_equal(area2, area)
+    assert [r[1] for r in decile_table(pr2, area2)] == [float(pr[np.argmax(pr <= p)])
+                                                       for p in np.linspace(0.05, 0.95, 19)]
 
 
 def test_deterministic_capturezone_runs():

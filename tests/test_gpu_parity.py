@@ -182,6 +182,33 @@ def test_fit_matches_reference_goldens():
         assert np.allclose(cov, d[f"cov_{i}"], rtol=1e-8, atol=0), i
 
 
+def test_construct_fit_and_compute_fit_match_reference():
+    """Model.construct_fit runs oneka_fit_rows and Model.compute_fit runs
+    oneka_fit_solve (FP64 on the device); both against the reference's own
+    construct_fit / compute_fit outputs on the same inputs."""
+    from onekapy_gb300.model import Model, RangeError
+    d = golden("fit_rows_cases.npz")
+    for i in range(int(d["ncases"])):
+        w = [tuple(r) for r in golden("fit_cases.npz")[f"wells_{i}"]]
+        f = golden("fit_cases.npz")
+        mo = Model(float(f[f"base_{i}"]), float(f[f"K_{i}"]), 0.25, float(f[f"H_{i}"]), w)
+        obs = [tuple(r) for r in f[f"obs_{i}"]]
+        WA, Wb = mo.construct_fit(obs, float(d[f"xo_{i}"]), float(d[f"yo_{i}"]))
+        assert isinstance(WA, np.ndarray) and WA.shape == d[f"WA_{i}"].shape and Wb.shape == d[f"Wb_{i}"].shape
+        assert np.allclose(WA, d[f"WA_{i}"], rtol=1e-14, atol=0), i
+        assert np.allclose(Wb, d[f"Wb_{i}"], rtol=1e-12, atol=1e-12), i
+        ev, cov = Model.compute_fit(d[f"WA_{i}"], d[f"Wb_{i}"])
+        assert ev.shape == (6, 1) and cov.shape == (6, 6)
+        assert np.allclose(ev, d[f"ev_{i}"], rtol=1e-8, atol=0), i
+        assert np.allclose(cov, d[f"cov_{i}"], rtol=1e-8, atol=0), i
+    # an observed head at the base raises like the reference's construct_fit
+    with pytest.raises(RangeError):
+        mo.construct_fit([(10.0, 20.0, mo.base, 0.1)] + obs, 0.0, 0.0)
+    # a rank-deficient problem raises LinAlgError
+    with pytest.raises(np.linalg.LinAlgError):
+        Model.compute_fit(np.ones((10, 6)), np.ones((10, 1)))
+
+
 def test_realize_draws_match_philox_restatement(oracle_mod):
     """Integer Philox streams and uniform/triangular variates are bit-exact;
     lognormal (log/cos/exp) within 1e-14 relative."""
@@ -253,9 +280,9 @@ def test_rasterize_and_register_match_reference():
         pf.rasterize(list(pts[:, 0]), list(pts[:, 1]), umbra)
         assert (pf.xmin, pf.ymin, pf.nrows, pf.ncols) == (xmin, ymin, int(nrows), int(ncols))
         want = np.unpackbits(d[f"rgrid_{i}"])[: int(nrows) * int(ncols)].reshape(int(nrows), int(ncols))
-        assert np.array_equal(pf.rgrid.cpu().numpy(), want.astype(bool)), i
+        assert np.array_equal(pf.rgrid, want.astype(bool)), i
         pf.register(0.5)
-        assert np.array_equal(pf.pgrid.cpu().numpy(), 0.5 * want)
+        assert np.array_equal(pf.pgrid, 0.5 * want)
         assert not pf.rgrid.any()
 
 
