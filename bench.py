@@ -69,7 +69,7 @@ def args_():
     ap.add_argument("--nreal", type=int, default=10000)
     ap.add_argument("--npaths", type=int, default=1000)
     ap.add_argument("--fp64-sample", type=int, default=None,
-                    help="realizations of the FP64 comparison (config2: 200; config4: all)")
+                    help="realizations of the FP64 comparison (default: all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"])
     ap.add_argument("--fraction", type=float, default=1.0,
@@ -301,36 +301,32 @@ def run_ours(a):
 
     line = None
     if rank == 0:
-        # plain FP64 GPU tracker and the FP32 build on the same sample of realizations
-        n64 = min(a.fp64_sample or 200, R)
+        # the plain FP64 GPU tracker on every realization of the step (timed like a step) ...
+        n64 = min(a.fp64_sample or R, R)
         step(o64, min(8, n64))
         torch.cuda.synchronize()
         e64 = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         step(o64, n64, ev=e64)
         torch.cuda.synchronize()
-        c64 = counts.clone()
         fp64_rate = n64 / (e64[0].elapsed_time(e64[2]) / 1e3)
-        step(o32, n64)
-        torch.cuda.synchronize()
-        c32 = counts.clone()
-        linf = float((c32 - c64).abs().max().item()) / n64
-        mism = float(((c32 > 0) != (c64 > 0)).sum().item()) / max(1, int((c64 > 0).sum().item()))
+        # ... and the FP32 build against it, realization by realization and trace by trace
+        cmps, grids = fp32_vs_fp64(site, real.slice(0, n64), release, {"fp32": o32}, o64, grid, spec.spacing)
+        cmp = cmps["fp32"]
+        if n64 == R:
+            assert torch.equal(grids["fp32"], counts32_full), "mark-only counts differ from the step's counts"
 
         # end to end through the public API with host buffers
         from onekapy_gb300.stochastic import create_stochastic_capturezone
         e2e_n = R
 
-        # the result is read into pinned host memory, allocated once outside the timed calls
-        host_buf = torch.empty((grid.nrows, grid.ncols), dtype=torch.float64, pin_memory=True)
-
+        # the reference's caller reads pf.pgrid, a host float64 array (copied back from the device)
         def e2e_once():
             pf = create_stochastic_capturezone(0, P, spec.duration, e2e_n, spec.base, spec.c_dist,
                                                spec.p_dist, spec.t_dist, spec.wells, spec.observations,
                                                spec.spacing, spec.umbra, spec.confined, spec.tol,
                                                spec.maxstep, seed=SEED, precision=C.FP32,
                                                window=spec.half, chunk=R)
-            host_buf.copy_(pf.pgrid)
-            return host_buf.numpy(), pf
+            return pf.pgrid, pf
 
         e2e_once()
         torch.cuda.synchronize()
@@ -365,10 +361,9 @@ def run_ours(a):
                 "particle_steps_per_s": psteps,
                 "step_breakdown_ms": {"realize_fp64": float(np.mean(realize_ms)),
                                       "track_chronicle_fp32": float(np.mean(track_ms))},
-                "fp64_gpu": {"realizations_per_s": fp64_rate, "sample_realizations": n64,
+                "fp64_gpu": {"realizations_per_s": fp64_rate, "realizations": n64,
                              "speedup_fp32_over_fp64": value / world / fp64_rate},
-                "fp32_vs_fp64": {"linf_capture_probability": linf, "mismatched_visited_fraction": mism,
-                                 "sample_realizations": n64},
+                "fp32_vs_fp64": cmp,
                 "work_per_step": dict(zip(E.COUNTER_NAMES[:7], counters[:7])),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak / 1e12,
                              "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
@@ -390,6 +385,95 @@ def run_ours(a):
         dist.destroy_process_group()
     if line is not None:
         print(json.dumps(line))
+
+
+def popcount32(x):
+    """Set bits of each int32 word (SWAR, on the device; wraps like C)."""
+    x = x - ((x >> 1) & 0x55555555)
+    x = (x & 0x33333333) + ((x >> 2) & 0x33333333)
+    x = (x + (x >> 4)) & 0x0F0F0F0F
+    return (x * 0x01010101) >> 24
+
+
+def fp32_vs_fp64(site, real, release, variants, o64, grid, spacing, chunk=1000):
+    """FP32 builds (`variants`: name -> options) against the FP64 build on
+    every realization of `real` and every trace, outside any timed region.
+    All run in mark-only mode (realization k's traces ORed into its own
+    bitmask), so the comparison is per realization: the visited-node sets of
+    the two builds are XORed and counted.  The count grids are the bitmasks
+    summed over realizations.
+
+    Per variant: the capture-probability L-inf (resolution 1/R), the summed
+    count difference over the FP64 counts, the fraction of per-realization
+    node visits that differ (popcount of the XOR over the FP64 popcount; its
+    largest value in any one realization too), the endpoint drift in cells
+    over every trace that ended normally in both builds, and how many traces
+    took the same numbers of attempted and accepted steps.  Also returns the
+    count grids of each variant."""
+    import torch
+    from onekapy_gb300 import _capi as C
+    from onekapy_gb300 import engine as E
+    dev = site.device
+    R, P = real.n, release.shape[0]
+    slot_words = grid.slot_bytes() // 4
+    mwords = grid.nrows * grid.words_per_row
+    names = list(variants) + ["fp64"]
+    cnt = {k: torch.zeros((grid.nrows, grid.words_per_row * 32), dtype=torch.int64, device=dev) for k in names}
+    acc = {k: {"xor": 0, "ref": 0, "worst": 0.0, "drift": [], "same": 0, "status": 0} for k in variants}
+    for a in range(0, R, chunk):
+        b = min(R, a + chunk)
+        sub = real.slice(a, b)
+        masks, outs = {}, {}
+        for name in names:
+            o = o64 if name == "fp64" else variants[name]
+            masks[name] = torch.zeros((b - a, slot_words), dtype=torch.int32, device=dev)
+            outs[name] = E.TrackOutputs.alloc(b - a, P, dev, endpoint=True, stats=True)
+            E.track(site, sub, release, o, grid, mark_only=masks[name], outputs=outs[name])
+            v = masks[name][:, :mwords].view(b - a, grid.nrows, grid.words_per_row)
+            for bit in range(32):
+                cnt[name][:, bit::32] += ((v >> bit) & 1).sum(dim=0)
+        m64, o64_ = masks["fp64"][:, :mwords], outs["fp64"]
+        r = popcount32(m64).sum(dim=1)
+        for name in variants:
+            A, o = acc[name], outs[name]
+            x = popcount32(masks[name][:, :mwords] ^ m64).sum(dim=1)
+            A["xor"] += int(x.sum().item())
+            A["ref"] += int(r.sum().item())
+            A["worst"] = max(A["worst"], float((x.double() / r.clamp(min=1).double()).max().item()))
+            ok = (o.status == C.TRACE_OK) & (o64_.status == C.TRACE_OK)
+            A["status"] += int((o.status == o64_.status).sum().item())
+            A["drift"].append(((o.endpoint - o64_.endpoint).norm(dim=-1) / spacing)[ok].float())
+            A["same"] += int(((o.naccept == o64_.naccept) & (o.nattempt == o64_.nattempt)).sum().item())
+        del masks, outs
+    c64 = cnt["fp64"][:, :grid.ncols]
+    res, grids = {}, {}
+    for name in variants:
+        A = acc[name]
+        c = cnt[name][:, :grid.ncols]
+        dr = torch.cat(A["drift"]) if A["drift"] else torch.zeros(0, device=dev)
+        # torch.quantile takes at most 2^24 elements: quantiles of the sorted drift by index
+        srt = torch.sort(dr).values
+        q = [float(srt[min(srt.numel() - 1, int(round(f * (srt.numel() - 1))))].item()) for f in (0.5, 0.99, 0.999)] \
+            if srt.numel() else [0.0] * 3
+        res[name] = {
+            "realizations": R, "traces": R * P,
+            "linf_capture_probability": float((c - c64).abs().max().item()) / R,
+            "linf_resolution": 1.0 / R,
+            "cells_above_0.01": int(((c - c64).abs().double() / R > 0.01).sum().item()),
+            "sum_abs_count_diff_over_sum64": float((c - c64).abs().sum().item()) / max(1, int(c64.sum().item())),
+            "mismatched_visit_fraction": A["xor"] / max(1, A["ref"]),
+            "mismatched_visit_fraction_worst_realization": A["worst"],
+            "fp64_visits": A["ref"],
+            "endpoint_drift_cells": {"p50": q[0], "p99": q[1], "p999": q[2],
+                                     "max": float(dr.max().item()) if dr.numel() else 0.0,
+                                     "traces_over_1e-3": int((dr > 1e-3).sum().item()),
+                                     "traces_over_1e-2": int((dr > 1e-2).sum().item()),
+                                     "traces_compared": int(dr.numel())},
+            "status_agreement": A["status"] / (R * P),
+            "traces_with_same_step_counts": A["same"] / (R * P)}
+        grids[name] = c.to(torch.int32)
+    grids["fp64"] = c64.to(torch.int32)
+    return res, grids
 
 
 def _hbm_roofline(dram_bytes, seconds):
@@ -604,66 +688,43 @@ def run_config4(a):
         E.track(site, real, release, o32, grid, counts=counts, scratch=scratch)
 
     ms, clocks = _timed(step32, a, stream, flush)
-    n64 = min(a.fp64_sample or R, R)
-    sub = real.slice(0, n64)
+    t = float(np.mean(ms)) / 1e3
     o32h = E.TrackOptions(**{**o32.__dict__, "head64": True})
-    res = {}
-    for name, o in (("fp32", o32), ("fp64", o64), ("fp32_head64", o32h)):
+    # speeds: the FP32 build with the FP64 head inversion on every realization, the FP64 build on a
+    # sample (its rate; about 100 realizations/s here)
+    secs, outs = {}, {}
+    for name, o, n in (("fp32", o32, R), ("fp32_head64", o32h, R), ("fp64", o64, min(R, 1000))):
         c = torch.zeros_like(counts)
-        out = E.TrackOutputs.alloc(n64, P, dev, endpoint=True, stats=True, counters=True)
+        out = E.TrackOutputs(counters=torch.zeros(E.COUNTERS, dtype=torch.int64, device=dev))
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        E.track(site, sub, release, o, grid, counts=c, scratch=scratch, outputs=out)
+        E.track(site, real.slice(0, n), release, o, grid, counts=c, scratch=scratch, outputs=out)
         e1.record()
         torch.cuda.synchronize()
-        res[name] = (c, out, e0.elapsed_time(e1) / 1e3)
-    c32, out32, t32 = res["fp32"]
-    c64, out64, t64 = res["fp64"]
-
-    def vs64(c, out):
-        d = (c - c64).abs().double() / n64
-        okp = (out.status == C.TRACE_OK) & (out64.status == C.TRACE_OK)
-        dr = ((out.endpoint - out64.endpoint).norm(dim=-1) / spec.spacing)[okp]
-        qq = torch.quantile(dr.float(), torch.tensor([0.5, 0.99], device=dev)).tolist() if dr.numel() else [0, 0]
-        return {"linf_capture_probability": float(d.max().item()), "cells_above_0.01": int((d > 0.01).sum().item()),
-                "drift_p50_cells": qq[0], "drift_p99_cells": qq[1],
-                "drift_max_cells": float(dr.max().item()) if dr.numel() else 0.0}
-
-    c32h, out32h, t32h = res["fp32_head64"]
-    diff = (c32 - c64).abs().double() / n64
-    visited = (c64 > 0) | (c32 > 0)
-    ok = (out32.status == C.TRACE_OK) & (out64.status == C.TRACE_OK)
-    drift = ((out32.endpoint - out64.endpoint).norm(dim=-1) / spec.spacing)[ok]
-    q = torch.quantile(drift.float(), torch.tensor([0.5, 0.99, 0.999], device=dev)).tolist() if drift.numel() else [0, 0, 0]
-    status_agree = float((out32.status == out64.status).double().mean().item())
-    t = float(np.mean(ms)) / 1e3
-    steps = int(out32.counters[1].item()) * R / n64
-    flops = algorithmic_flops(site.nwells, spec.confined, int(out32.counters[0].item()),
-                              int(out32.counters[2].item())) * R / n64
+        secs[name] = (e0.elapsed_time(e1) / 1e3, n)
+        outs[name] = out
+    # errors against the FP64 build on every realization and trace
+    n64 = min(a.fp64_sample or R, R)
+    cmps, _ = fp32_vs_fp64(site, real.slice(0, n64), release, {"fp32": o32, "fp32_head64": o32h}, o64, grid,
+                           spec.spacing)
+    cnt32 = outs["fp32"].counters
+    steps = int(cnt32[1].item())
+    flops = algorithmic_flops(site.nwells, spec.confined, int(cnt32[0].item()), int(cnt32[2].item()))
+    fp64_rate = secs["fp64"][1] / secs["fp64"][0]
     cfg = {"workload": "config4-unconfined-31wells: 5000 realizations x 2048 paths, 25 y, 5 m grid 8x8 km",
-           "nreal": R, "npaths": P, "fp64_realizations": n64, "l2": "512 MB buffer written between timed steps"}
+           "nreal": R, "npaths": P, "fp64_realizations_compared": n64,
+           "l2": "512 MB buffer written between timed steps"}
     line = _line(a, R / t, UNIT, METRIC + " (unconfined stress)", cfg, ms_per_step=1e3 * t,
                  particle_steps_per_s=steps / t,
-                 roofline=fp32_roofline(flops, t, "track32_kernel (+ register_counts, realize); flops scaled from "
-                                                  f"the {n64}-realization counters"),
-                 fp64_gpu={"realizations_per_s": n64 / t64, "speedup_fp32_over_fp64": (R / t) / (n64 / t64)},
-                 fp32_vs_fp64_per_cell={"linf_capture_probability": float(diff.max().item()),
-                                        "mean_abs_over_visited_cells": float(diff[visited].mean().item())
-                                        if bool(visited.any()) else 0.0,
-                                        "cells_above_0.01": int((diff > 0.01).sum().item()),
-                                        "visited_cells": int(visited.sum().item()),
-                                        "mismatched_visited_fraction":
-                                            float(((c32 > 0) != (c64 > 0)).sum().item()) / max(1, int(visited.sum().item()))},
-                 endpoint_drift_cells={"p50": q[0], "p99": q[1], "p999": q[2],
-                                       "max": float(drift.max().item()) if drift.numel() else 0.0,
-                                       "within_1e-3_cell": float((drift <= 1e-3).double().mean().item())
-                                       if drift.numel() else 1.0,
-                                       "particles_compared": int(drift.numel())},
-                 status_agreement=status_agree,
+                 roofline=fp32_roofline(flops, t, "track32_kernel (+ register_counts, realize)"),
+                 fp64_gpu={"realizations_per_s": fp64_rate, "timed_realizations": secs["fp64"][1],
+                           "speedup_fp32_over_fp64": (R / t) / fp64_rate},
+                 fp32_vs_fp64=cmps["fp32"],
                  fp32_head64={"note": "general path with heads within 1 % of the aquifer top re-inverted in FP64",
-                              "seconds_fp64_sample": t32h, "seconds_fp32_sample": t32,
-                              "vs_fp64": vs64(c32h, out32h), "fp32_vs_fp64": vs64(c32, out32)},
+                              "seconds_all_realizations": secs["fp32_head64"][0],
+                              "seconds_fp32_all_realizations": secs["fp32"][0],
+                              "vs_fp64": cmps["fp32_head64"]},
                  tracker_launch={"block": o32.block, "occupancy": o32.occupancy, "window_kb": o32.window_kb},
                  clocks=clocks)
     print(json.dumps(line))

@@ -291,9 +291,14 @@ ONEKA_API int oneka_track_batched(const OnekaTrackJob* jobs, int32_t njobs, void
  *   - Every call on a device shares the array and clears the part it uses
  *     first; calls that overlap on the GPU (other streams or threads) race on
  *     it, so order them on one stream.
+ *   - The array is reserved on a device when the library's device code is
+ *     first loaded there, i.e. at the first call on that device, not when the
+ *     library is loaded.  A host whose own allocator takes the GPU after its
+ *     set-up should make one call during that set-up.
  *   - The first call on each device (with that device current) looks up the
  *     array's device address and caches it; make that first call before any
- *     stream capture.
+ *     stream capture.  A cudaDeviceReset invalidates the cached address: it
+ *     is not supported while the library is in use.
  */
 ONEKA_API int oneka_track_noalloc(const OnekaSite* site, const OnekaRealizations* real, int32_t nreal,
                                   const double* release, int32_t npaths, const OnekaTrackOpts* opts,

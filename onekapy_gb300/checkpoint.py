@@ -3,8 +3,9 @@
 The reference only archives a finished run (oneka/archive.py:46-89); a run
 that stops early is lost.  Here a run on a fixed window can be saved after
 every chunk of realizations and resumed later.  The state is small: the int32
-count grid, the number of registered realizations and the index of the next
-realization.  Resuming is exact -- the realization draws are Philox streams
+count grid, the number of registered realizations, the index of the next
+realization and the run's trace counters (attempts, accepted steps, chronicle
+work, DRY / STEP_LIMIT traces, traces leaving the grid).  Resuming is exact -- the realization draws are Philox streams
 keyed by (seed, realization index), so realization k is the same whichever
 call draws it, and integer counts add exactly -- so an interrupted and
 resumed run returns the same counts as an uninterrupted one.
@@ -21,7 +22,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-FORMAT = 1
+FORMAT = 2
+NCOUNTERS = 8
 
 
 def _canon(v):
@@ -54,6 +56,11 @@ class RunState:
     registered: int             # realizations registered so far
     next_realization: int       # first realization not yet tracked
     nrealizations: int
+    counters: np.ndarray | None = None   # int64 [8] trace counters summed so far
+
+    def __post_init__(self):
+        if self.counters is None:
+            self.counters = np.zeros(NCOUNTERS, dtype=np.int64)
 
     @property
     def complete(self) -> bool:
@@ -66,7 +73,8 @@ class RunState:
             np.savez(f, format=np.int64(FORMAT), signature=np.array(self.signature),
                      counts=np.ascontiguousarray(self.counts, dtype=np.int32),
                      registered=np.int64(self.registered), next_realization=np.int64(self.next_realization),
-                     nrealizations=np.int64(self.nrealizations))
+                     nrealizations=np.int64(self.nrealizations),
+                     counters=np.ascontiguousarray(self.counters, dtype=np.int64))
             f.flush()
             os.fsync(f.fileno())
         os.replace(tmp, path)
@@ -77,7 +85,8 @@ class RunState:
             if int(z["format"]) != FORMAT:
                 raise ValueError(f"{path}: checkpoint format {int(z['format'])}, expected {FORMAT}")
             return RunState(str(z["signature"]), z["counts"].astype(np.int32), int(z["registered"]),
-                            int(z["next_realization"]), int(z["nrealizations"]))
+                            int(z["next_realization"]), int(z["nrealizations"]),
+                            z["counters"].astype(np.int64))
 
 
 def open_state(path: str | None, sig: str, shape, nrealizations: int) -> RunState:

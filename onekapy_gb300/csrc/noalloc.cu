@@ -7,8 +7,13 @@
 // they reach the GPU through a binding that only passes buffers the host
 // already owns.  oneka_track_noalloc serves them from a fixed array that lives
 // inside this library instead: g_noalloc_slots below, ONEKA_NOALLOC_SCRATCH_BYTES
-// (32 MiB).  Every GPU that loads the library holds that array until the
-// process exits.
+// (32 MiB).  The CUDA runtime loads this library's device code lazily, on its
+// first use on a device, so the array is reserved on a device at the first
+// call there (the first oneka_track_noalloc, or any other first launch of the
+// library on that device), not when the library is loaded.  A host that hands
+// the rest of the GPU to its own allocator should make one call during its own
+// set-up, before that allocator takes the memory.  The array is then held until
+// the process exits.
 //
 // The array is shared by every call on a device and keeps what the last call
 // left in it; each call clears the slots it is about to use before tracking.
@@ -19,8 +24,10 @@
 // Host code may not use g_noalloc_slots as a pointer: in host code the name
 // is a host-side stand-in, not the device address.  The first call on each
 // device, with that device current, asks the runtime for the array's device
-// address (cudaGetSymbolAddress) and caches it; that first call should come
-// before any stream capture.
+// address (cudaGetSymbolAddress) and caches it for the process; that first call
+// should come before any stream capture.  A cudaDeviceReset (or any teardown
+// of the device's primary context) unloads the array and leaves the cached
+// address stale: it is not supported while this library is in use.
 #include <mutex>
 
 #include "oneka_internal.cuh"

@@ -7,6 +7,13 @@
 //     the particle position is a float pair (hi + lo) updated with an
 //     error-free two-sum, so the position keeps ~48 bits over hundreds of
 //     steps;
+//   * every well's position is a float pair too, and its distance to the
+//     particle is differenced pair by pair, (x_hi - xw_hi) + (x_lo - xw_lo):
+//     the high difference is exact near the well (Sterbenz), so r^2 about
+//     each well keeps the particle's full position, not one rounded to a
+//     float (the recentred r^2);
+//   * x and y travel together as packed FP32 pairs (Blackwell's FADD2 /
+//     FMUL2 / FFMA2), one instruction for both coordinates;
 //   * the discharge's well terms are summed with Kahan compensation (the
 //     potential's too in the FP64 head-inversion mode);
 //   * the head is inverted from the compensated potential in FP32 (the
@@ -33,8 +40,19 @@
 namespace oneka {
 namespace {
 
+// Packed FP32 pairs: (x, y) in one 64-bit register pair, one instruction for
+// both (FADD2 / FMUL2 / FFMA2 on sm_100 and later); every operation rounds
+// each lane once, as its scalar form does.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// b - a with one rounding (a * -1 is exact).
+__device__ __forceinline__ float2 rsub2(float2 a, float2 b) { return __ffma2_rn(a, make_float2(-1.0f, -1.0f), b); }
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+
 struct Model32 {
-    const float4* w;     // per well: x, y (relative to the target), -q/(2 pi), q ln(2)/(4 pi)
+    const float4* wp;    // per well: -x_hi, -y_hi, -x_lo, -y_lo (relative to the target)
+    const float2* wq;    // per well: -q/(2 pi), q ln(2)/(4 pi)
     int nw;
     float ox, oy;        // regional origin relative to the target
     float c0, c1, c2, c3, c4, c5;
@@ -56,54 +74,66 @@ struct Kahan {
     }
 };
 
+// Kahan summation of (x, y) pairs; the compensation is kept negated, so the
+// total is s + cn and every step is one packed instruction.
+struct Kahan2 {
+    float2 s, cn;
+    __device__ __forceinline__ void add_prod(float2 a, float2 b) {   // += a * b
+        const float2 y = fma2(a, b, cn);
+        const float2 t = add2(s, y);
+        cn = rsub2(rsub2(s, t), y);     // y - (t - s)
+        s = t;
+    }
+};
+
 // Velocity modes of the FP32 build: the general (mixed) path, the confined
 // path, and the general path with the optional FP64 near-top head inversion.
 enum Mode32 { kGeneral = 0, kConfined = 1, kGeneralHead64 = 2 };
 
+// -V at the point ph + pl (hi and lo parts of x and y), in k.  Returns false
+// at a dry point (potential or head <= 0, the reference's AquiferError).
 template <int MODE>
-__device__ __forceinline__ bool feval32(const Model32& m, float x, float y, float& kx, float& ky) {
+__device__ __forceinline__ bool feval32(const Model32& m, float2 ph, float2 pl, float2& k) {
     constexpr bool CONFINED = MODE == kConfined;
-    const float dxo = x - m.ox;
-    const float dyo = y - m.oy;
-    Kahan qx{-(2.0f * m.c0 * dxo + m.c2 * dyo + m.c3), 0.0f};
-    Kahan qy{-(2.0f * m.c1 * dyo + m.c2 * dxo + m.c4), 0.0f};
+    const float2 p = add2(ph, pl);                 // the point rounded to floats, for the regional terms
+    const float dxo = p.x - m.ox;
+    const float dyo = p.y - m.oy;
+    Kahan2 q{make_float2(-(2.0f * m.c0 * dxo + m.c2 * dyo + m.c3), -(2.0f * m.c1 * dyo + m.c2 * dxo + m.c4)),
+             make_float2(0.0f, 0.0f)};
     Kahan pot{0.0f, 0.0f};
     if (!CONFINED)
         pot.s = m.c0 * dxo * dxo + m.c1 * dyo * dyo + m.c2 * dxo * dyo + m.c3 * dxo + m.c4 * dyo + m.c5;
 #pragma unroll 4
     for (int i = 0; i < m.nw; ++i) {
-        const float4 w = m.w[i];
-        const float dx = x - w.x;
-        const float dy = y - w.y;
-        const float r2 = dx * dx + dy * dy;
-        const float s = __fdividef(w.z, r2);
-        qx.add(s * dx);
-        qy.add(s * dy);
-        // q/(4 pi) ln r^2 (ln 2 folded into w.w).  The discharge sums above
+        const float4 w = m.wp[i];
+        const float2 wq = m.wq[i];
+        // recentred difference: (x_hi - xw_hi) + (x_lo - xw_lo), both coordinates at once
+        const float2 d = add2(add2(ph, make_float2(w.x, w.y)), add2(pl, make_float2(w.z, w.w)));
+        const float r2 = d.x * d.x + d.y * d.y;
+        q.add_prod(splat(__fdividef(wq.x, r2)), d);
+        // q/(4 pi) ln r^2 (ln 2 folded into wq.y).  The discharge sums above
         // carry the trace's accuracy and are compensated; the potential only
         // selects the head branch and scales the velocity, and compensating
         // it changed no measured drift, so it is compensated only where the
         // FP64 head inversion reads the unrounded pair.
         if (!CONFINED) {
             if (MODE == kGeneralHead64)
-                pot.add(w.w * __log2f(r2));
+                pot.add(wq.y * __log2f(r2));
             else
-                pot.s += w.w * __log2f(r2);
+                pot.s += wq.y * __log2f(r2);
         }
     }
+    const float2 qt = add2(q.s, q.cn);
     if (CONFINED) {
-        kx = -((qx.s - qx.c) * m.inv_hn);
-        ky = -((qy.s - qy.c) * m.inv_hn);
+        k = mul2(qt, splat(-m.inv_hn));
         return true;
     }
-    // Head from the compensated potential (model.py:341-350).  The inversion
-    // itself is well conditioned (sqrt halves relative errors; the confined
-    // branch is linear), so FP32 keeps the digits the compensated sum
-    // delivers.  An FP64 inversion near the aquifer top would add nothing to
-    // an FP32 result and, on GB300, costs the whole warp ~1000 FP64-pipe
-    // cycles whenever one lane takes it.  Computed without branches; a dry
-    // point (potential or head <= 0, the reference's AquiferError) is
-    // reported through the return value.
+    // Head from the potential (model.py:341-350).  The inversion itself is
+    // well conditioned (sqrt halves relative errors; the confined branch is
+    // linear), so FP32 keeps the digits the potential delivers.  An FP64
+    // inversion near the aquifer top would add nothing to an FP32 result and,
+    // on GB300, costs the whole warp ~1000 FP64-pipe cycles whenever one lane
+    // takes it.  Computed without branches.
     const float phi = pot.s - pot.c;
     const float kh2 = m.kh2f;
     const float hu = sqrtf(fmaxf(2.0f * phi * m.inv_k, 0.0f));
@@ -114,21 +144,26 @@ __device__ __forceinline__ bool feval32(const Model32& m, float x, float y, floa
         // optional: the inversion in FP64 from the unrounded compensated pair
         // (model.py:341-350 operation order)
         const double K = m.d64[0], n = m.d64[1], H = m.d64[2];
-        const double ph = (double)pot.s - (double)pot.c;
-        const double h = (ph < 0.5 * K * H * H) ? sqrt(2.0 * ph / K) : (ph + 0.5 * K * H * H) / (K * H);
+        const double ph64 = (double)pot.s - (double)pot.c;
+        const double h = (ph64 < 0.5 * K * H * H) ? sqrt(2.0 * ph64 / K) : (ph64 + 0.5 * K * H * H) / (K * H);
         head = (float)h;
         inv = (h > H) ? m.inv_hn : (float)(1.0 / (h * n));
     }
-    kx = -((qx.s - qx.c) * inv);
-    ky = -((qy.s - qy.c) * inv);
+    k = mul2(qt, splat(-inv));
     return (phi > 0.0f) && (head > 0.0f);
 }
 
-// Error-free a + b = s + e (Knuth's two-sum).
+// Error-free a + b = s + e (Knuth's two-sum), scalar and for (x, y) pairs.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+    s = add2(a, b);
+    const float2 bb = rsub2(a, s);                           // s - a
+    e = add2(rsub2(rsub2(bb, s), a), rsub2(bb, b));          // (a - (s - bb)) + (b - bb)
 }
 
 // Conversions without the FP64 pipe.  On GB300, I2F/F2I and float rounding
@@ -223,23 +258,28 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
                                          int fncols, int fnrows, float fx0, float fy0, const Raster32& g,
                                          float ax, float ay, float bx, float by, unsigned& ntest,
                                          unsigned& natom, int& rlo, int& rhi) {
+    // the grid constants live in shared memory next to the window that the
+    // row loop ORs into; registers copies keep them from being reloaded
+    // after every atomic
+    const float umbra = g.umbra, inv_dx = g.inv_dx, inv_dy = g.inv_dy;
+    const float U = g.U, U2 = g.U2, ryy = g.ryy;
     const float bax = bx - ax;
     const float bay = by - ay;
     if (!(bax * bax + bay * bay > 0.0f)) return;    // the reference's 0/0 marks nothing
     int left, right, bottom, top;
-    if (!clip_int(floor_small((fminf(ax, bx) - g.umbra - fx0) * g.inv_dx),
-                  floor_small((fmaxf(ax, bx) + g.umbra - fx0) * g.inv_dx) + 1, fncols, left, right))
+    if (!clip_int(floor_small((fminf(ax, bx) - umbra - fx0) * inv_dx),
+                  floor_small((fmaxf(ax, bx) + umbra - fx0) * inv_dx) + 1, fncols, left, right))
         return;
-    if (!clip_int(floor_small((fminf(ay, by) - g.umbra - fy0) * g.inv_dy),
-                  floor_small((fmaxf(ay, by) + g.umbra - fy0) * g.inv_dy) + 1, fnrows, bottom, top))
+    if (!clip_int(floor_small((fminf(ay, by) - umbra - fy0) * inv_dy),
+                  floor_small((fmaxf(ay, by) + umbra - fy0) * inv_dy) + 1, fnrows, bottom, top))
         return;
     ntest += (unsigned)(right - left) * (unsigned)(top - bottom);
     // segment in units of dx: X from column 0 of the frame, Y from row 0
-    const float aX = (ax - fx0) * g.inv_dx, aY = (ay - fy0) * g.inv_dx;
-    const float bX = (bx - fx0) * g.inv_dx, bY = (by - fy0) * g.inv_dx;
+    const float aX = (ax - fx0) * inv_dx, aY = (ay - fy0) * inv_dx;
+    const float bX = (bx - fx0) * inv_dx, bY = (by - fy0) * inv_dx;
     const float BAX = bX - aX, BAY = bY - aY;
     const float L2 = BAX * BAX + BAY * BAY;
-    const float UL = g.U * sqrtf(L2);
+    const float UL = U * sqrtf(L2);
     // band |BAY s - BAX t| < U L (t = row offset from a, s = X - aX):
     //   s in (k t - |e|, k t + |e|), k = BAX / BAY, e = U L / BAY
     // projection 0 <= BAX s + BAY t <= L^2:
@@ -262,14 +302,14 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     // the shared-memory window (almost every segment near the target) the
     // marks go there without per-row or per-word window tests.
     auto rows = [&](auto in_win) {
-        float t = i2f_small(rb) * g.ryy - aY;           // row offset from a (units of dx)
-        for (int i = rb; i < re; ++i, t += g.ryy) {
+        float t = i2f_small(rb) * ryy - aY;             // row offset from a (units of dx)
+        for (int i = rb; i < re; ++i, t += ryy) {
             const int gi = i + roff;
             float LO = INFINITY, HI = -INFINITY;
-            const float ha = g.U2 - t * t;
+            const float ha = U2 - t * t;
             if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
             const float tb = t - BAY;
-            const float hb = g.U2 - tb * tb;
+            const float hb = U2 - tb * tb;
             if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bX - h); HI = fmaxf(HI, bX + h); }
             float slo, shi;
             if (bay_nz) {
@@ -277,7 +317,7 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
                 slo = kt - ae;
                 shi = kt + ae;
             } else {
-                const bool in = fabsf(t) < g.U;
+                const bool in = fabsf(t) < U;
                 slo = in ? -INFINITY : INFINITY;
                 shi = in ? INFINITY : -INFINITY;
             }
@@ -313,29 +353,45 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
 // Dormand-Prince tableau in FP32 (capturezone.py:202-209), arranged for
 // running sums.  Row s = 0..5 is the stage point of k_{s+2} (row 5 is the
 // 5th-order solution).  After k_{j+1} (j = 0..5) is evaluated it is added
-// into every later row: P_s += c_dp_b[j][s] * k, where c_dp_b[j][s] is
+// into every later row: P_s += dp_b(j, s) * k, where dp_b(j, s) is
 // a[s][j+1] for s > j and 0 otherwise, and into the error sum with
-// c_dp_e[j+1] (k7 = f(xyt) carries -1/40, the reference's e[1]).
-__constant__ float c_dp_a0[6] = {(float)DP::a2, (float)DP::a31, (float)DP::a41, (float)DP::a51,
-                                 (float)DP::a61, (float)DP::a71};
-__constant__ float c_dp_b[6][6] = {
-    {0, (float)DP::a32, (float)DP::a42, (float)DP::a52, (float)DP::a62, 0.0f},
-    {0, 0, (float)DP::a43, (float)DP::a53, (float)DP::a63, (float)DP::a73},
-    {0, 0, 0, (float)DP::a54, (float)DP::a64, (float)DP::a74},
-    {0, 0, 0, 0, (float)DP::a65, (float)DP::a75},
-    {0, 0, 0, 0, 0, (float)DP::a76},
-    {0, 0, 0, 0, 0, 0}};
-__constant__ float c_dp_e[7] = {(float)DP::e1, 0.0f, (float)DP::e3, (float)DP::e4, (float)DP::e5,
-                                (float)DP::e6, (float)DP::e2};
+// dp_e(j + 1) (k7 = f(xyt) carries -1/40, the reference's e[1]).  The values
+// are compile-time constants, so the zero entries cost nothing.
+__device__ __forceinline__ constexpr float dp_a0(int s) {
+    return s == 0 ? (float)DP::a2 : s == 1 ? (float)DP::a31 : s == 2 ? (float)DP::a41
+         : s == 3 ? (float)DP::a51 : s == 4 ? (float)DP::a61 : (float)DP::a71;
+}
+__device__ __forceinline__ constexpr float dp_b(int j, int s) {
+    return j == 0 ? (s == 1 ? (float)DP::a32 : s == 2 ? (float)DP::a42 : s == 3 ? (float)DP::a52
+                   : s == 4 ? (float)DP::a62 : 0.0f)
+         : j == 1 ? (s == 2 ? (float)DP::a43 : s == 3 ? (float)DP::a53 : s == 4 ? (float)DP::a63
+                   : s == 5 ? (float)DP::a73 : 0.0f)
+         : j == 2 ? (s == 3 ? (float)DP::a54 : s == 4 ? (float)DP::a64 : s == 5 ? (float)DP::a74 : 0.0f)
+         : j == 3 ? (s == 4 ? (float)DP::a65 : s == 5 ? (float)DP::a75 : 0.0f)
+         : j == 4 ? (s == 5 ? (float)DP::a76 : 0.0f)
+         : 0.0f;
+}
+__device__ __forceinline__ constexpr float dp_e(int i) {
+    return i == 0 ? (float)DP::e1 : i == 1 ? 0.0f : i == 2 ? (float)DP::e3 : i == 3 ? (float)DP::e4
+         : i == 4 ? (float)DP::e5 : i == 5 ? (float)DP::e6 : (float)DP::e2;
+}
 
 struct RealConst32 {
-    float c0, c1, c2, c3, c4, c5, K, n, H, inv_hn, ox, oy, kh2f, inv_k, inv_kh;
+    // what every velocity evaluation reads, as three 16-byte shared-memory loads
+    float4 q0;           // c0, c1, c2, c3 (A..D)
+    float4 q1;           // c4, c5, ox, oy (E, F, regional origin)
+    float4 q2;           // inv_hn, kh2f, inv_k, inv_kh
+    float K, n, H;
     double d64[3];       // K, n, H in FP64 for the optional near-top head inversion
     float tol, maxstep;  // options, converted once
     Raster32 g;          // grid constants of the chronicle
     int skip;
     int next;            // next particle of this block's chunk
 };
+
+// float4 slots of a block's well arrays: positions [nw] float4, then
+// constants [nw] float2 rounded up to whole float4s.
+__host__ __device__ __forceinline__ int well_float4s(int nw) { return nw + (nw + 1) / 2; }
 
 // Per-lane particle state.  Everything the step loop touches is FP32: on
 // GB300 the FP64 pipe runs at ~1/64 of the FP32 rate, so a handful of FP64
@@ -348,8 +404,9 @@ struct Particle32 {
     int p;               // particle index, >= pend when the lane is out of work
     int status, att;
     float tau_h, tau_l;  // duration - t
-    float dt, xh, xl, yh, yl;
-    float k1x, k1y;      // f at the current point (first stage, FSAL)
+    float dt;
+    float2 ph, pl;       // position (x, y): hi and lo parts
+    float2 k1;           // f at the current point (first stage, FSAL)
 };
 
 // Shared-memory columns of the per-lane cold state: field f of lane t at
@@ -370,17 +427,19 @@ struct Cold {
 
 // The realization's constants come from shared memory (block-uniform).
 template <int MODE>
-__device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* w, int nw, float x, float y,
-                                        float& kx, float& ky) {
+__device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* wp, const float2* wq, int nw,
+                                        float2 ph, float2 pl, float2& k) {
     Model32 m;
-    m.w = w;
+    m.wp = wp;
+    m.wq = wq;
     m.nw = nw;
-    m.ox = rc.ox; m.oy = rc.oy;
-    m.c0 = rc.c0; m.c1 = rc.c1; m.c2 = rc.c2; m.c3 = rc.c3; m.c4 = rc.c4; m.c5 = rc.c5;
-    m.K = rc.K; m.n = rc.n; m.H = rc.H; m.inv_hn = rc.inv_hn; m.kh2f = rc.kh2f;
-    m.inv_k = rc.inv_k; m.inv_kh = rc.inv_kh;
+    const float4 q0 = rc.q0, q1 = rc.q1, q2 = rc.q2;
+    m.c0 = q0.x; m.c1 = q0.y; m.c2 = q0.z; m.c3 = q0.w;
+    m.c4 = q1.x; m.c5 = q1.y; m.ox = q1.z; m.oy = q1.w;
+    m.inv_hn = q2.x; m.kh2f = q2.y; m.inv_k = q2.z; m.inv_kh = q2.w;
+    m.K = rc.K; m.n = rc.n; m.H = rc.H;
     m.d64 = rc.d64;
-    return feval32<MODE>(m, x, y, kx, ky);
+    return feval32<MODE>(m, ph, pl, k);
 }
 
 // Write the finished particle's outputs.
@@ -389,8 +448,8 @@ __device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Part
                                          const Chron& ch) {
     const long long idx = (long long)r * L.npaths + s.p;
     if (L.out.endpoint) {
-        L.out.endpoint[2 * idx] = L.xt + ((double)s.xh + (double)s.xl);
-        L.out.endpoint[2 * idx + 1] = L.yt + ((double)s.yh + (double)s.yl);
+        L.out.endpoint[2 * idx] = L.xt + ((double)s.ph.x + (double)s.pl.x);
+        L.out.endpoint[2 * idx + 1] = L.yt + ((double)s.ph.y + (double)s.pl.y);
     }
     if (L.out.bbox) {
         L.out.bbox[4 * idx] = L.xt + (double)c.f(kBx0);
@@ -414,8 +473,8 @@ __device__ __forceinline__ void push_vertex(const TrackLaunch& L, int r, const P
     const int nv = c.i(kNv);
     if (L.out.vertices && nv < L.out.max_vertices) {
         double* v = L.out.vertices + ((long long)r * L.npaths + s.p) * 2LL * L.out.max_vertices;
-        v[2 * nv] = L.xt + ((double)s.xh + (double)s.xl);
-        v[2 * nv + 1] = L.yt + ((double)s.yh + (double)s.yl);
+        v[2 * nv] = L.xt + ((double)s.ph.x + (double)s.pl.x);
+        v[2 * nv + 1] = L.yt + ((double)s.ph.y + (double)s.pl.y);
     }
     c.i(kNv) = nv + 1;
 }
@@ -424,13 +483,11 @@ __device__ __forceinline__ void push_vertex(const TrackLaunch& L, int r, const P
 // false when the trace is already over (dry at the release point, or a zero
 // duration).
 template <int MODE, int BLOCK>
-__device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealConst32& rc, const float4* w,
-                                        Particle32& s, const Cold<BLOCK>& c) {
+__device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealConst32& rc, const float4* wp,
+                                        const float2* wq, Particle32& s, const Cold<BLOCK>& c) {
     const double rx = L.release[2 * s.p] - L.xt, ry = L.release[2 * s.p + 1] - L.yt;
-    s.xh = (float)rx;
-    s.yh = (float)ry;
-    s.xl = (float)(rx - (double)s.xh);
-    s.yl = (float)(ry - (double)s.yh);
+    s.ph = make_float2((float)rx, (float)ry);
+    s.pl = make_float2((float)(rx - (double)s.ph.x), (float)(ry - (double)s.ph.y));
     const OnekaFrame f = frame_of(L, r, s.p);
     c.f(kFx0) = (float)(f.xmin - L.xt);
     c.f(kFy0) = (float)(f.ymin - L.yt);
@@ -450,24 +507,23 @@ __device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealC
     s.tau_h = (float)dur;
     s.tau_l = (float)(dur - (double)s.tau_h);
     s.dt = 0.1f * (dur > 0.0 ? 1.0f : (dur < 0.0 ? -1.0f : 0.0f));
-    c.f(kBx0) = c.f(kBx1) = s.xh + s.xl;
-    c.f(kBy0) = c.f(kBy1) = s.yh + s.yl;
+    const float2 p0 = add2(s.ph, s.pl);
+    c.f(kBx0) = c.f(kBx1) = p0.x;
+    c.f(kBy0) = c.f(kBy1) = p0.y;
     push_vertex<BLOCK>(L, r, s, c);
-    float kx, ky;
-    if (!feval_c<MODE>(rc, w, L.nwells, s.xh + s.xl, s.yh + s.yl, kx, ky)) {
+    if (!feval_c<MODE>(rc, wp, wq, L.nwells, s.ph, s.pl, s.k1)) {
         s.status = ONEKA_TRACE_DRY;
         return false;
     }
-    s.k1x = kx;
-    s.k1y = ky;
     return s.tau_h != 0.0f;
 }
 
 // One step attempt of the Dormand-Prince integrator (capturezone.py:221-247).
 // Returns false when the trace is over.
 template <int MODE, int BLOCK>
-__device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst32& rc, const float4* w,
-                                          const Chron& ch, Particle32& s, int r, const Cold<BLOCK>& c) {
+__device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst32& rc, const float4* wp,
+                                          const float2* wq, const Chron& ch, Particle32& s, int r,
+                                          const Cold<BLOCK>& c) {
     if (s.att >= L.max_attempts) {
         s.status = ONEKA_TRACE_STEP_LIMIT;
         return false;
@@ -481,41 +537,33 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
         last = true;
     }
     const float dt = s.dt;
+    const float2 DT = splat(dt);
     // running sums of the stage rows and of the error row, seeded with k1
-    float px[6], py[6];
+    float2 P[6];
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        px[q] = c_dp_a0[q] * s.k1x;
-        py[q] = c_dp_a0[q] * s.k1y;
-    }
-    float ex = c_dp_e[0] * s.k1x, ey = c_dp_e[0] * s.k1y;
-    float kx = 0.0f, ky = 0.0f;
+    for (int q = 0; q < 6; ++q) P[q] = mul2(splat(dp_a0(q)), s.k1);
+    float2 E = mul2(splat(dp_e(0)), s.k1);
+    float2 k = make_float2(0.0f, 0.0f);
     bool wet = true;
 #pragma unroll
     for (int st = 0; st < 6; ++st) {            // evaluates k2..k7 (unrolled: stage rows are compile-time)
-        // px[st] selected with compile-time indexes only
-        float ax = px[0], ay = py[0];
-#pragma unroll
-        for (int q = 1; q < 6; ++q)
-            if (q == st) { ax = px[q]; ay = py[q]; }
         // a dry stage ends the trace after the attempt (nothing of it is kept)
-        wet &= feval_c<MODE>(rc, w, L.nwells, s.xh + (s.xl + dt * ax), s.yh + (s.yl + dt * ay), kx, ky);
+        wet &= feval_c<MODE>(rc, wp, wq, L.nwells, s.ph, fma2(DT, P[st], s.pl), k);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            px[q] += c_dp_b[st][q] * kx;
-            py[q] += c_dp_b[st][q] * ky;
-        }
-        ex += c_dp_e[st + 1] * kx;
-        ey += c_dp_e[st + 1] * ky;
+        for (int q = st + 1; q < 6; ++q)
+            if (dp_b(st, q) != 0.0f) P[q] = fma2(splat(dp_b(st, q)), k, P[q]);
+        E = fma2(splat(dp_e(st + 1)), k, E);
     }
     if (!wet) {
         s.status = ONEKA_TRACE_DRY;
         return false;
     }
-    // kx, ky = k7 = f(xyt); the 5th-order step is dt * P_5
-    const float sx = dt * px[5], sy = dt * py[5];
-    const float est = fmaxf(fabsf(dt * ex), fabsf(dt * ey));
-    const float ds = sqrtf(sx * sx + sy * sy);
+    // k = k7 = f(xyt); the 5th-order step is dt * P_5
+    const float2 S = mul2(DT, P[5]);
+    const float2 Ed = mul2(DT, E);
+    const float est = fmaxf(fabsf(Ed.x), fabsf(Ed.y));
+    const float2 S2 = mul2(S, S);
+    const float ds = sqrtf(S2.x + S2.y);
     const float tol = rc.tol, maxstep = rc.maxstep, eps = (float)DP::eps;
     if ((est < tol) && (ds < maxstep)) {
         if (last) {
@@ -526,32 +574,24 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
             te += s.tau_l;
             two_sum(th, te, s.tau_h, s.tau_l);
         }
-        const float ax = s.xh + s.xl, ay = s.yh + s.yl;
-        float q, e;
-        two_sum(s.xh, sx, q, e);
-        s.xl += e;
-        two_sum(q, s.xl, s.xh, e);
-        s.xl = e;
-        two_sum(s.yh, sy, q, e);
-        s.yl += e;
-        two_sum(q, s.yl, s.yh, e);
-        s.yl = e;
-        const float bxn = s.xh + s.xl, byn = s.yh + s.yl;
+        const float2 a = add2(s.ph, s.pl);
+        float2 q, e;
+        two_sum2(s.ph, S, q, e);
+        two_sum2(q, add2(s.pl, e), s.ph, s.pl);
+        const float2 b = add2(s.ph, s.pl);
         if (ch.slot) {
             unsigned ntest = (unsigned)c.i(kNtest), natom = (unsigned)c.i(kNatom);
             int rlo = c.i(kRlo), rhi = c.i(kRhi);
             insert32(ch, L.grid.nrows, L.grid.ncols, c.i(kCoff), c.i(kRoff), c.i(kNcols), c.i(kNrows),
-                     c.f(kFx0), c.f(kFy0), rc.g, ax, ay,
-                     bxn, byn, ntest, natom, rlo, rhi);
+                     c.f(kFx0), c.f(kFy0), rc.g, a.x, a.y, b.x, b.y, ntest, natom, rlo, rhi);
             c.i(kNtest) = (int)ntest;
             c.i(kNatom) = (int)natom;
             c.i(kRlo) = rlo;
             c.i(kRhi) = rhi;
         }
-        c.f(kBx0) = fminf(c.f(kBx0), bxn); c.f(kBx1) = fmaxf(c.f(kBx1), bxn);
-        c.f(kBy0) = fminf(c.f(kBy0), byn); c.f(kBy1) = fmaxf(c.f(kBy1), byn);
-        s.k1x = kx;
-        s.k1y = ky;
+        c.f(kBx0) = fminf(c.f(kBx0), b.x); c.f(kBx1) = fmaxf(c.f(kBx1), b.x);
+        c.f(kBy0) = fminf(c.f(kBy0), b.y); c.f(kBy1) = fmaxf(c.f(kBy1), b.y);
+        s.k1 = k;
         push_vertex<BLOCK>(L, r, s, c);
         c.i(kAcc) += 1;
     }
@@ -569,9 +609,10 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     extern __shared__ float4 sm32[];
     __shared__ RealConst32 rc;
     const int r = L.r0 + k;
-    float4* w = sm32;
+    float4* wp = sm32;                                        // [nwells] positions (hi, lo), negated
+    float2* wq = reinterpret_cast<float2*>(sm32 + L.nwells);  // [nwells] well constants
     Cold<BLOCK> cold;
-    cold.base = reinterpret_cast<uint32_t*>(sm32 + L.nwells);
+    cold.base = reinterpret_cast<uint32_t*>(sm32 + well_float4s(L.nwells));
     uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
     const Chron ch = make_chron(L, slot, cold.base + kColdFields * BLOCK);
     // particles [pbeg, pend) of this block
@@ -581,13 +622,11 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     if (threadIdx.x == 0) {
         const double* c = L.coef + 6LL * r;
         const double Kd = L.aquifer[3LL * r], nd = L.aquifer[3LL * r + 1], Hd = L.aquifer[3LL * r + 2];
-        rc.c0 = (float)c[0]; rc.c1 = (float)c[1]; rc.c2 = (float)c[2];
-        rc.c3 = (float)c[3]; rc.c4 = (float)c[4]; rc.c5 = (float)c[5];
+        rc.q0 = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
+        rc.q1 = make_float4((float)c[4], (float)c[5], (float)(L.xo - L.xt), (float)(L.yo - L.yt));
+        rc.q2 = make_float4((float)(1.0 / (Hd * nd)), (float)(0.5 * Kd * (Hd * Hd)), (float)(1.0 / Kd),
+                            (float)(1.0 / (Kd * Hd)));
         rc.K = (float)Kd; rc.n = (float)nd; rc.H = (float)Hd;
-        rc.inv_hn = (float)(1.0 / (Hd * nd));
-        rc.kh2f = (float)(0.5 * Kd * (Hd * Hd));
-        rc.inv_k = (float)(1.0 / Kd);
-        rc.inv_kh = (float)(1.0 / (Kd * Hd));
         rc.d64[0] = Kd; rc.d64[1] = nd; rc.d64[2] = Hd;
         rc.tol = (float)L.opts.tol;
         rc.maxstep = (float)L.opts.maxstep;
@@ -599,17 +638,17 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
         rc.g.U2 = rc.g.U * rc.g.U;
         rc.g.ryy = (float)(L.grid.dy / L.grid.dx);
         rc.g.umbra = (float)L.opts.umbra;
-        rc.ox = (float)(L.xo - L.xt);
-        rc.oy = (float)(L.yo - L.yt);
         rc.skip = L.rstatus && L.rstatus[r] != ONEKA_REAL_OK;
         rc.next = pbeg + BLOCK;
         if (!rc.skip && chunk == 0 && L.registered) atomicAdd(L.registered, 1ull);
     }
     for (int i = threadIdx.x; i < L.nwells; i += BLOCK) {
         const double q = L.q[(long long)r * L.nwells + i];
-        w[i] = make_float4((float)(L.wells[3 * i] - L.xt), (float)(L.wells[3 * i + 1] - L.yt),
-                           (float)(-q * 0.15915494309189535),
-                           (float)(q * (0.07957747154594767 * 0.69314718055994531)));
+        const double dx = L.wells[3 * i] - L.xt, dy = L.wells[3 * i + 1] - L.yt;
+        const float xh = (float)dx, yh = (float)dy;
+        wp[i] = make_float4(-xh, -yh, -(float)(dx - (double)xh), -(float)(dy - (double)yh));
+        wq[i] = make_float2((float)(-q * 0.15915494309189535),
+                            (float)(q * (0.07957747154594767 * 0.69314718055994531)));
     }
     window_clear(ch);
     __syncthreads();
@@ -624,7 +663,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     bool live = false;
     // start this lane's first particle; a lane whose trace ends at once takes the next
     while (s.p < pend && !live) {
-        live = start32<MODE, BLOCK>(L, r, rc, w, s, cold);
+        live = start32<MODE, BLOCK>(L, r, rc, wp, wq, s, cold);
         if (!live) {
             finish32<BLOCK>(L, r, s, cold, ch);
             s.p = atomicAdd(&rc.next, 1);
@@ -635,11 +674,11 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     // the next stage evaluations in separate groups.  BLOCK is a multiple of 32.
     while (__any_sync(0xffffffffu, live)) {
         if (!live) continue;
-        live = attempt32<MODE, BLOCK>(L, rc, w, ch, s, r, cold);
+        live = attempt32<MODE, BLOCK>(L, rc, wp, wq, ch, s, r, cold);
         while (!live && s.p < pend) {
             finish32<BLOCK>(L, r, s, cold, ch);
             s.p = atomicAdd(&rc.next, 1);
-            if (s.p < pend) live = start32<MODE, BLOCK>(L, r, rc, w, s, cold);
+            if (s.p < pend) live = start32<MODE, BLOCK>(L, r, rc, wp, wq, s, cold);
         }
     }
     __syncthreads();
@@ -693,7 +732,7 @@ cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
         if (chunks > maxc) chunks = maxc;
         if (chunks < 1) chunks = 1;
     }
-    const size_t smem = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)kColdFields * BLOCK +
+    const size_t smem = sizeof(float4) * (size_t)well_float4s(L.nwells) + 4 * (size_t)kColdFields * BLOCK +
                         4 * (size_t)L.win_rows * L.win_words;
     auto kern = track32_kernel<MODE, BLOCK, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -759,7 +798,7 @@ cudaError_t launch_track32_batch(const JobTable& T, int rows, cudaStream_t s) {
     size_t smem = 0;
     for (int j = 0; j < T.njobs; ++j) {
         const TrackLaunch& L = T.job[j];
-        const size_t need = sizeof(float4) * (size_t)L.nwells + 4 * (size_t)kColdFields * block +
+        const size_t need = sizeof(float4) * (size_t)well_float4s(L.nwells) + 4 * (size_t)kColdFields * block +
                             4 * (size_t)L.win_rows * L.win_words;
         if (need > smem) smem = need;
     }

@@ -122,6 +122,8 @@ def create_stochastic_capturezone(
         registered.fill_(state.registered)
         first = state.next_realization
     counters = torch.zeros(E.COUNTERS, dtype=torch.int64, device=dev)
+    if state is not None:          # the resumed run's counters continue the saved ones
+        counters.copy_(torch.from_numpy(state.counters))
     out = E.TrackOutputs(counters=counters)
     done_chunks = 0
     a = first
@@ -138,6 +140,7 @@ def create_stochastic_capturezone(
         if state is not None:
             state.counts = counts.cpu().numpy()
             state.registered = int(registered.item())
+            state.counters = counters.cpu().numpy()
             state.next_realization = a
             state.save(checkpoint)
     pfield.counts = counts

@@ -27,7 +27,7 @@ def golden_opts(d, precision, head64=False):
                           head64=head64)
 
 
-def run_golden(d, precision, max_vertices=None, slots=None, head64=False):
+def run_golden(d, precision, max_vertices=None, slots=None, head64=False, release_shift=None):
     dev = C.device()
     site = golden_site(d, dev)
     real = golden_real(d, dev)
@@ -37,7 +37,8 @@ def run_golden(d, precision, max_vertices=None, slots=None, head64=False):
     out = E.TrackOutputs.alloc(nreal, npaths, dev, bbox=True, max_vertices=mv)
     counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
     reg = torch.zeros(1, dtype=torch.int64, device=dev)
-    E.track(site, real, torch.as_tensor(d["release"], device=dev), golden_opts(d, precision, head64), grid,
+    release = d["release"] if release_shift is None else d["release"] + np.asarray(release_shift)
+    E.track(site, real, torch.as_tensor(release, device=dev), golden_opts(d, precision, head64), grid,
             counts=counts, registered=reg, outputs=out, slots=slots)
     torch.cuda.synchronize()
     return dict(counts=counts.cpu().numpy(), registered=int(reg.item()),

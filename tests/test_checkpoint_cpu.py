@@ -29,13 +29,15 @@ def test_signature_is_stable_and_sensitive():
 
 def test_state_round_trip_and_atomic_write(tmp_path):
     path = str(tmp_path / "run.npz")
-    st = CK.RunState("abc", np.arange(12, dtype=np.int32).reshape(3, 4), 5, 8, 40)
+    st = CK.RunState("abc", np.arange(12, dtype=np.int32).reshape(3, 4), 5, 8, 40,
+                     np.array([100, 90, 7, 6, 1, 0, 2, 0], dtype=np.int64))
     st.save(path)
     assert sorted(os.listdir(tmp_path)) == ["run.npz"]          # no temporary left behind
     got = CK.RunState.load(path)
     assert got.signature == "abc" and got.registered == 5 and got.next_realization == 8
     assert got.nrealizations == 40 and not got.complete
     assert got.counts.dtype == np.int32 and np.array_equal(got.counts, st.counts)
+    assert got.counters.dtype == np.int64 and np.array_equal(got.counters, st.counters)
 
 
 def test_open_state_fresh_resume_and_mismatch(tmp_path):

@@ -93,39 +93,121 @@ def test_config1_full_fp64_bit_exact_vs_oracle(oracle_mod):
     assert linf <= 0.01, linf
 
 
-def test_config2_subset_fp64_bit_exact_vs_oracle(oracle_mod):
-    """Config 2 site (mixed aquifer, general head path), 24 realizations x 200 paths."""
-    spec = S.config2(nreal=24, npaths=200)
+def _track(site, real, spec, grid, precision, release=None, head64=False):
+    """One oneka_track call: host counts, registered count, and per-trace
+    endpoint / naccept / nattempt / status."""
+    dev = site.device
+    rel = site.release(spec.npaths) if release is None else release
+    out = E.TrackOutputs.alloc(real.n, spec.npaths, dev)
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+    reg = torch.zeros(1, dtype=torch.int64, device=dev)
+    opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=spec.confined, precision=precision, head64=head64)
+    E.track(site, real, torch.as_tensor(rel, device=dev), opts, grid, counts=counts, registered=reg, outputs=out)
+    torch.cuda.synchronize()
+    return counts.cpu().numpy(), int(reg.item()), {k: getattr(out, k).cpu().numpy()
+                                                   for k in ("endpoint", "naccept", "nattempt", "status")}
+
+
+# The FP32 build's endpoint bar, trace by trace.  A trace is well conditioned
+# when its FP64 endpoint moves less than WELL_CONDITIONED_CELLS (cells) as its
+# release point moves 1 nm (an amplification below 5,000).  Every well-
+# conditioned trace must end within 1e-3 cell of the FP64 build.  The others
+# pass a neighbour well's stagnation zone, where the FP64 trace itself moves
+# by the FP32 build's error under a displacement of about a micrometre: each
+# must end within 20 times the distance its FP64 endpoint moves when the
+# release point moves 100 nm (measured on 4.1 M traces of the unconfined
+# stress site: at most 14 times).
+WELL_CONDITIONED_CELLS = 1e-6
+
+
+def _fp32_bars(site, real, spec, grid, c64, o64, ill_fraction_max, ntrace_real=None):
+    """The FP32 build against the FP64 build's counts c64 and outputs o64 on
+    `real`: L-inf over all realizations, the per-trace bars on the first
+    ntrace_real realizations (default all)."""
+    R = real.n
+    n = R if ntrace_real is None else min(R, ntrace_real)
+    c32, _, o32 = _track(site, real, spec, grid, C.FP32)
+    linf = np.abs(c32.astype(np.int64) - c64).max() / R
+    assert linf <= 0.01, linf
+    rel = site.release(spec.npaths)
+    sub = real.slice(0, n)
+    _, _, o1 = _track(site, sub, spec, grid, C.FP64, release=rel + np.array([1e-9, 0.0]))
+    _, _, o100 = _track(site, sub, spec, grid, C.FP64, release=rel + np.array([1e-7, 0.0]))
+    o32 = {k: v[:n] for k, v in o32.items()}
+    o64 = {k: v[:n] for k, v in o64.items()}
+    ok = (o32["status"] == C.TRACE_OK) & (o64["status"] == C.TRACE_OK)
+    assert np.array_equal(o32["status"], o64["status"])
+    cell = spec.spacing
+    drift = np.linalg.norm(o32["endpoint"] - o64["endpoint"], axis=-1)[ok] / cell
+    sens1 = np.linalg.norm(o1["endpoint"] - o64["endpoint"], axis=-1)[ok] / cell
+    sens100 = np.linalg.norm(o100["endpoint"] - o64["endpoint"], axis=-1)[ok] / cell
+    well = sens1 <= WELL_CONDITIONED_CELLS
+    assert drift[well].max() <= 1e-3, drift[well].max()
+    assert np.all(drift <= np.maximum(1e-3, 20.0 * sens100)), np.max(drift / np.maximum(sens100, 1e-30))
+    assert (~well).mean() <= ill_fraction_max, (~well).mean()
+    return drift, well
+
+
+def test_config2_200x1000_fp64_bit_exact_fp32_every_trace(oracle_mod):
+    """Config 2 site (mixed aquifer, general head path), 200 realizations x
+    1,000 paths: FP64 counts, registrations and step counts equal the
+    oracle's; the FP32 build within the bars on every trace, L-inf <= 0.01."""
+    spec = S.config2(nreal=200, npaths=1000)
     site = _site(spec)
     real = E.realize(site, spec.nreal, seed=1002)
     grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
-    out = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
-    got, reg = _gpu_counts(site, real, spec, grid, C.FP64, outputs=out)
+    got, reg, o64 = _track(site, real, spec, grid, C.FP64)
     want = _oracle_counts(oracle_mod, site, real, spec, grid)
-    assert reg == want["registered"]
-    assert np.array_equal(out.naccept.cpu().numpy(), want["naccept"])
+    assert reg == want["registered"] == spec.nreal
+    assert np.array_equal(o64["naccept"], want["naccept"])
     assert np.array_equal(got, want["counts"]), f"{(got != want['counts']).sum()} nodes differ"
+    drift, well = _fp32_bars(site, real, spec, grid, got, o64, ill_fraction_max=0.001)
+    assert drift.max() <= 1e-3, drift.max()          # every trace of this site is within the bar
 
 
-def test_config4_subset_fp64_vs_oracle_and_fp32(oracle_mod):
-    """Config 4 (thin unconfined, 31 wells): FP64 parity and the FP32 precision split."""
-    spec = S.config4(nreal=12, npaths=128)
+def test_config4_100x2048_fp64_bit_exact_fp32_every_trace(oracle_mod):
+    """Config 4 (thin unconfined, 31 wells), 100 realizations x 2,048 paths:
+    FP64 against the oracle, and the FP32 build (with and without the FP64
+    head inversion near the aquifer top) within the bars on every trace."""
+    spec = S.config4(nreal=100, npaths=2048)
     site = _site(spec)
     real = E.realize(site, spec.nreal, seed=1004)
     ok = real.status.cpu().numpy() == 0
     grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
-    out64 = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
-    got, reg = _gpu_counts(site, real, spec, grid, C.FP64, outputs=out64)
+    got, reg, o64 = _track(site, real, spec, grid, C.FP64)
     want = _oracle_counts(oracle_mod, site, real, spec, grid)
-    assert reg == int(ok.sum())
+    assert reg == int(ok.sum()) == want["registered"]
+    assert np.array_equal(o64["naccept"], want["naccept"])
     assert np.array_equal(got, want["counts"]), f"{(got != want['counts']).sum()} nodes differ"
-    for head64 in (False, True):      # FP32 head inversion, and the FP64 one near the aquifer top
-        out32 = E.TrackOutputs.alloc(spec.nreal, spec.npaths, site.device)
-        got32, _ = _gpu_counts(site, real, spec, grid, C.FP32, outputs=out32, head64=head64)
-        same = (out32.naccept == out64.naccept).cpu().numpy() & (out64.status == 0).cpu().numpy()
-        drift = (out32.endpoint - out64.endpoint).abs().amax(dim=2).cpu().numpy()[same]
-        assert np.percentile(drift, 99) <= 1e-3 * spec.spacing, (head64, np.percentile(drift, 99))
-        assert np.abs(got32 - got).max() / max(reg, 1) <= 0.1
+    _fp32_bars(site, real, spec, grid, got, o64, ill_fraction_max=0.02)
+    c32h, _, _ = _track(site, real, spec, grid, C.FP32, head64=True)
+    assert np.abs(c32h.astype(np.int64) - got).max() / max(reg, 1) <= 0.01
+
+
+# Four of the 64 batched sites: the most wells (192) with 4,096 paths over
+# 49 years, 175 wells on a 768^2 grid at 5 m, the fewest wells (2), and a
+# 360-path site with 148 wells.
+CONFIG3_SITES = [43, 59, 23, 14]
+
+
+@pytest.mark.parametrize("k", CONFIG3_SITES)
+def test_config3_sites_fp64_bit_exact_and_fp32(oracle_mod, k):
+    """Config 3 sites: FP64 counts of 4 realizations equal the oracle's; the
+    FP32 build against FP64 on 200 realizations: L-inf <= 0.01 and the
+    per-trace bars."""
+    spec = S.config3()[k]
+    site = _site(spec)
+    grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+    small = E.realize(site, 4, seed=3000 + k)
+    got, reg, o64 = _track(site, small, spec, grid, C.FP64)
+    want = _oracle_counts(oracle_mod, site, small, spec, grid)
+    assert reg == want["registered"]
+    assert np.array_equal(o64["naccept"], want["naccept"])
+    assert np.array_equal(got, want["counts"]), f"site {k}: {(got != want['counts']).sum()} nodes differ"
+    real = E.realize(site, 200, seed=3000 + k)
+    c64, _, o64 = _track(site, real, spec, grid, C.FP64)
+    _fp32_bars(site, real, spec, grid, c64, o64, ill_fraction_max=0.02, ntrace_real=40)
 
 
 def test_create_stochastic_capturezone_dropin(oracle_mod):
@@ -224,6 +306,7 @@ def test_checkpoint_resume_equals_uninterrupted_run(tmp_path):
     rest = create_stochastic_capturezone(*args, **kw, checkpoint=path)
     assert rest.complete and rest.total_weight == 12.0
     assert torch.equal(rest.counts, full.counts)
+    assert rest.trace_counters == full.trace_counters        # the counters resume too
     done = create_stochastic_capturezone(*args, **kw, checkpoint=path)     # nothing left to do
     assert done.complete and torch.equal(done.counts, full.counts)
     with pytest.raises(ValueError, match="different inputs"):

@@ -4,8 +4,11 @@ Bars:
   * FP64 build: visit counts bit-exact; vertices equal to the reference's
     (bit-exact except where libm pow/log and CUDA pow/log round a step
     factor or a logarithm differently, then within 1e-9 relative).
-  * FP32 build: endpoints within 1e-3 of the cell size of the FP64 build for
-    traces that took the same steps; capture-probability L-inf <= 0.01.
+  * FP32 build, on every trace: the endpoint within 1e-3 of the cell size of
+    the FP64 build's wherever the FP64 trace is well conditioned (its
+    endpoint moves less than 1e-6 cell when the release point moves 1 nm),
+    and within 20 times the FP64 endpoint's own movement under a 100 nm
+    release displacement everywhere; capture-probability L-inf <= 0.01.
 """
 import numpy as np
 import pytest
@@ -73,10 +76,18 @@ def test_fp32_drift_and_probability(case, head64):
     d = golden(f"track_{case}.npz")
     r64 = run_golden(d, C.FP64)
     r32 = run_golden(d, C.FP32, head64=head64)
-    same = r32["naccept"] == r64["naccept"]
-    assert same.mean() >= 0.9
-    drift = np.abs(r32["endpoint"] - r64["endpoint"]).max(axis=2)[same]
-    assert drift.max() <= 1e-3 * float(d["spacing"]), drift.max()
+    s1 = run_golden(d, C.FP64, release_shift=[1e-9, 0.0])
+    s100 = run_golden(d, C.FP64, release_shift=[1e-7, 0.0])
+    ok = (r32["status"] == C.TRACE_OK) & (r64["status"] == C.TRACE_OK)
+    assert np.array_equal(r32["status"], r64["status"])
+    cell = float(d["spacing"])
+    drift = np.linalg.norm(r32["endpoint"] - r64["endpoint"], axis=-1)[ok] / cell
+    sens1 = np.linalg.norm(s1["endpoint"] - r64["endpoint"], axis=-1)[ok] / cell
+    sens100 = np.linalg.norm(s100["endpoint"] - r64["endpoint"], axis=-1)[ok] / cell
+    well = sens1 <= 1e-6
+    assert well.mean() >= 0.95
+    assert drift[well].max() <= 1e-3, drift[well].max()
+    assert np.all(drift <= np.maximum(1e-3, 20.0 * sens100))
     R = int(d["total_weight"])
     linf = np.abs(r32["counts"] - r64["counts"]).max() / R
     assert linf <= 0.01 + 1.0 / R  # at most one realization flips any node at this tiny R
@@ -244,6 +255,47 @@ def test_realize_draws_match_philox_restatement(oracle_mod):
     # shard invariance: drawing [first+10, first+20) alone gives the same realizations
     part = E.realize(site, 10, seed=seed, first=first + 10)
     assert torch.equal(part.coef, real.coef[10:20])
+
+
+@pytest.mark.parametrize("kind", ["uniform", "triangular", "lognormal"])
+def test_variates_match_numpy_distributions(kind):
+    """The realization draws (row a1) against the reference's generators:
+    10^6 Philox variates from oneka_realize, as well discharges of a
+    1,000-well site over 1,000 realizations, against 10^6 draws of NumPy's
+    legacy generator (np.random.uniform / np.random.triangular, the calls of
+    oneka/stochastic.py:297-304, and np.random.lognormal for the lognormal
+    extension).  Bars: mean within 0.2 % and variance within 1 % of NumPy's
+    and of the exact values (about 7 and 3.7 standard errors at n = 10^6); Kolmogorov-Smirnov D below 2.5 sqrt(2/n) = 0.0035 between
+    the two samples and below 2.5 / sqrt(n) = 0.0025 against the exact CDF
+    (n = 10^6; two samples of one distribution exceed these with probability
+    about 10^-5)."""
+    stats = pytest.importorskip("scipy.stats")
+    dev = C.device()
+    nw, nr = 1000, 1000
+    if kind == "uniform":
+        d, ref = (400.0, 600.0), np.random.RandomState(11).uniform(400.0, 600.0, nw * nr)
+        cdf = stats.uniform(400.0, 200.0).cdf
+        mean, var = 500.0, 200.0 ** 2 / 12
+    elif kind == "triangular":
+        d, ref = (100.0, 200.0, 500.0), np.random.RandomState(12).triangular(100.0, 200.0, 500.0, nw * nr)
+        cdf = stats.triang(c=0.25, loc=100.0, scale=400.0).cdf
+        mean = 800.0 / 3
+        var = (100.0 ** 2 + 200.0 ** 2 + 500.0 ** 2 - 100.0 * 200.0 - 100.0 * 500.0 - 200.0 * 500.0) / 18
+    else:
+        d, ref = E.Lognormal(np.log(10.0), 0.3), np.random.RandomState(13).lognormal(np.log(10.0), 0.3, nw * nr)
+        cdf = stats.lognorm(s=0.3, scale=10.0).cdf
+        mean = 10.0 * np.exp(0.045)
+        var = (np.exp(0.09) - 1) * np.exp(2 * np.log(10.0) + 0.09)
+    wells = [(float(i), 0.0, 0.25, d) for i in range(nw)]
+    site = E.Site(wells, np.zeros((0, 4)), 0.0, device=dev)
+    real = E.realize(site, nr, seed=977)
+    got = real.q.cpu().numpy().reshape(-1)
+    assert got.size == nw * nr and np.all(np.isfinite(got))
+    for m, v in ((got.mean(), got.var()), (ref.mean(), ref.var())):
+        assert abs(m - mean) <= 0.002 * mean and abs(v - var) <= 0.01 * var, (kind, m, v, mean, var)
+    assert abs(got.mean() - ref.mean()) <= 0.002 * mean and abs(got.var() - ref.var()) <= 0.01 * var
+    assert stats.ks_2samp(got, ref).statistic < 0.0035, kind
+    assert stats.kstest(got, cdf).statistic < 0.0025, kind
 
 
 def test_mvn_draw_statistics():

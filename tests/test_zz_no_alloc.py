@@ -76,6 +76,38 @@ def test_noalloc_matches_track_over_several_launches():
     _check_twice(site, real, torch.as_tensor(site.release(spec.npaths), device=dev), opts, grid)
 
 
+def test_noalloc_allocates_no_device_memory():
+    """The defining property: after a first call on the device (which loads
+    the library's module and with it the fixed array), further calls leave
+    the device's free memory and torch's allocations unchanged."""
+    spec = S.config1()
+    dev = C.device()
+    site = E.Site(spec.wells, spec.observations, spec.base, c_dist=spec.c_dist, p_dist=spec.p_dist,
+                  t_dist=spec.t_dist, device=dev)
+    real = E.realize(site, 8, seed=7)
+    grid = E.Grid.window(site.xt, site.yt, spec.spacing, spec.half)
+    opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=spec.confined, precision=C.FP32)
+    release = torch.as_tensor(site.release(24), device=dev)
+    counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+    reg = torch.zeros(1, dtype=torch.int64, device=dev)
+    args = [ctypes.byref(site.c()), ctypes.byref(real.c()), real.n, C.ptr(release), release.shape[0],
+            ctypes.byref(opts.c()), ctypes.byref(grid.c()), None, C.ptr(counts), C.ptr(reg), None,
+            C.stream_ptr()]
+    L = C.load()
+    C.check(L.oneka_track_noalloc(*args))         # the warm-up call a host makes at its own set-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    torch0 = torch.cuda.memory_allocated()
+    for _ in range(2):
+        C.check(L.oneka_track_noalloc(*args))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert torch.cuda.memory_allocated() == torch0
+    assert free1 == free0, (free0, free1)
+    assert int(reg.item()) == 3 * 8 and int(counts.sum().item()) > 0
+
+
 def test_noalloc_rejects_a_grid_beyond_its_array():
     d = golden("track_confined_u10.npz")
     dev = C.device()
