@@ -134,7 +134,7 @@ typedef struct OnekaTrackOpts {
     int32_t block;           /* threads per block: 32, 64, 128 or 256; 0: 256 (FP32), 128 (FP64) */
     int32_t window_kb;       /* shared-memory chronicle window per block in KiB (0: 32; < 0: none) */
     int32_t occupancy;       /* FP32 build: resident blocks per SM to compile for (4, 6, 8 at 128
-                                threads; 2, 3 at 256); 0: the lowest */
+                                threads; 2, 3, 4 at 256); 0: the lowest */
     int32_t head64;          /* FP32 build, general path: 1 re-inverts a head within 1 % of the
                                 aquifer top in FP64 from the compensated potential (off: FP32);
                                 runs the 256 x 3 launch shape; not for batched launches */
@@ -366,15 +366,20 @@ ONEKA_API int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nb
  * K % 32 == 0; lda, ldb, ldc % 8 == 0; matrices and bias 16-byte aligned.  splitk > 1 adds
  * partial products into a zeroed FP32 C (no GELU, no Z).
  *
- * K-major A and B with K % 64 == 0 and no split-K run on the tcgen05 kernel
- * (TMA-staged operands, accumulator in tensor memory; FP32 C, or BF16 C with
- * GELU and Z); everything else on an mma.sync kernel.  flags bit 0 forces the
- * mma.sync kernel.
+ * K-major A and B with K % 64 == 0 run on the tcgen05 kernel (TMA-staged
+ * operands, accumulator in tensor memory; FP32 C, also split-K, or BF16 C
+ * with GELU and Z); everything else on an mma.sync kernel.  flags bit 0
+ * forces the mma.sync kernel.
  */
 ONEKA_API int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B, int32_t ldb,
                               int32_t b_kmajor, void* C, int32_t ldc, int32_t c_f32, const float* bias,
                               int32_t gelu, void* Z, int32_t M, int32_t N, int32_t K, int32_t splitk,
                               int32_t flags, void* stream);
+
+/* dst[c][r] = src[r][c] for a BF16 matrix src [rows][lds] into dst [cols][ldd]: the backward
+ * GEMMs' operands turned K-major for the tcgen05 kernel. */
+ONEKA_API int oneka_transpose_bf16(const void* src, int32_t rows, int32_t cols, int64_t lds, void* dst, int64_t ldd,
+                                   void* stream);
 
 /* 1 when oneka_gemm_bf16 with these arguments runs on the tcgen05 kernel, else 0 (host only). */
 ONEKA_API int oneka_gemm_bf16_path(int32_t a_kmajor, int32_t b_kmajor, int32_t K, int32_t splitk, int32_t c_f32,
@@ -414,6 +419,13 @@ ONEKA_API int oneka_colsum_bf16(const void* x, int32_t rows, int32_t cols, float
 /* AdamW step `step` (>= 1) on FP32 w, m, v with gradient g; writes the BF16 copy w_bf16 if given. */
 ONEKA_API int oneka_adamw(float* w, float* m, float* v, const float* g, void* w_bf16, int64_t n, float lr,
                           float beta1, float beta2, float eps, float weight_decay, int32_t step, void* stream);
+
+/* oneka_adamw with the step's learning rate and bias corrections read from device memory,
+ * hyper = [lr, 1 - beta1^t, 1 - beta2^t], so that a training step captured in a CUDA graph
+ * follows a schedule written into hyper between replays. */
+ONEKA_API int oneka_adamw_scheduled(float* w, float* m, float* v, const float* g, void* w_bf16, int64_t n,
+                                    const float* hyper, float beta1, float beta2, float eps, float weight_decay,
+                                    void* stream);
 
 /* Standardized BF16 features [n][ld] of realizations: A..F, discharges, K, porosity (nf = 8 + nwells). */
 ONEKA_API int oneka_features(const double* coef, const double* q, const double* aquifer, int32_t nwells,

@@ -44,6 +44,10 @@ cudaError_t launch_adamw(float* w, float* m, float* v, const float* g, void* wb,
 cudaError_t launch_features(const double* coef, const double* q, const double* aquifer, int nwells, int n,
                             const float* mean, const float* inv_std, int nf, int ld, void* x, cudaStream_t s);
 cudaError_t launch_sigmoid_colsum(const float* logits, int rows, int cols, float* out, cudaStream_t s);
+cudaError_t launch_transpose_bf16(const void* src, int rows, int cols, long long lds, void* dst, long long ldd,
+                                  cudaStream_t s);
+cudaError_t launch_adamw_scheduled(float* w, float* m, float* v, const float* g, void* wb, long long n,
+                                   const float* hyper, float b1, float b2, float eps, float wd, cudaStream_t s);
 cudaError_t launch_evaluate(const OnekaSite& site, const double* q, double K, double n, double H,
                             const double* coef, const double* pts, long long npts, int confined,
                             double* potential, double* discharge, double* head, double* velocity,
@@ -448,6 +452,15 @@ int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B,
     return ONEKA_OK;
 }
 
+int oneka_transpose_bf16(const void* src, int32_t rows, int32_t cols, int64_t lds, void* dst, int64_t ldd,
+                         void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(src && dst && rows >= 0 && cols >= 0, "src/dst/rows/cols");
+    ONEKA_CHECK_ARG(lds >= cols && ldd >= rows, "leading dimensions");
+    ONEKA_CHECK_CUDA(launch_transpose_bf16(src, rows, cols, lds, dst, ldd, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
 int oneka_gemm_bf16_path(int32_t a_kmajor, int32_t b_kmajor, int32_t K, int32_t splitk, int32_t c_f32, int32_t gelu,
                          int32_t has_z, int32_t sigsum, int32_t flags) {
     return gemm_path(a_kmajor, b_kmajor, K, splitk, c_f32, gelu, has_z ? (void*)1 : nullptr,
@@ -504,6 +517,15 @@ int oneka_adamw(float* w, float* m, float* v, const float* g, void* w_bf16, int6
     ONEKA_CHECK_ARG(w && m && v && g && n >= 0 && step >= 1, "adamw arguments");
     ONEKA_CHECK_CUDA(launch_adamw(w, m, v, g, w_bf16, n, lr, beta1, beta2, eps, weight_decay, step,
                                   (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_adamw_scheduled(float* w, float* m, float* v, const float* g, void* w_bf16, int64_t n, const float* hyper,
+                          float beta1, float beta2, float eps, float weight_decay, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(w && m && v && g && hyper && n >= 0, "adamw arguments");
+    ONEKA_CHECK_CUDA(launch_adamw_scheduled(w, m, v, g, w_bf16, n, hyper, beta1, beta2, eps, weight_decay,
+                                            (cudaStream_t)stream));
     return ONEKA_OK;
 }
 

@@ -3,12 +3,14 @@
 // C[M][N] = A[M][K] * B[N][K]^T (both operands K-major, BF16; FP32
 // accumulation) for the layers of the surrogate MLP, with fused epilogues:
 // bias + FP32 store (logits), bias + GELU storing the pre-activation and the
-// activation in BF16 (hidden layers), and bias + sigmoid summed over the rows
-// (the screened capture field; C is never stored).
+// activation in BF16 (hidden layers), bias + sigmoid summed over the rows
+// (the screened capture field; C is never stored), and split-K, where each
+// K slice of a tile adds its partial product into a zeroed FP32 C (the
+// backward GEMMs whose K is the 65,536 outputs).
 //
-// A persistent, warp-specialized kernel: one CTA per SM walks 128 x 256
-// output tiles (M fastest, so consecutive tiles reuse the same B slice from
-// L2).
+// A persistent, warp-specialized kernel: one CTA per SM walks work items,
+// 128 x 256 output tiles (M fastest, so consecutive tiles reuse the same B
+// slice from L2), times the K slices of a split-K launch.
 //   * warp 0 (one lane): TMA producer.  cp.async.bulk.tensor with the 128-byte
 //     swizzle stages 64-wide K slices of A (128 x 64) and B (256 x 64) into a
 //     4-stage shared-memory ring; "full" mbarriers complete on the copies'
@@ -55,7 +57,7 @@ constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + alignment slack (
 constexpr int TMEM_COLS = 512;       // two 256-column accumulators
 constexpr unsigned long long kWaitNs = 2000000000ull;      // 2 s per wait
 
-enum TcEpilogue { kEpiF32 = 0, kEpiGelu = 1, kEpiSigsum = 2 };
+enum TcEpilogue { kEpiF32 = 0, kEpiGelu = 1, kEpiSigsum = 2, kEpiF32Add = 3 };
 
 struct TcArgs {
     void* C;              // kEpiF32: float [M][ldc]; kEpiGelu: bf16 H [M][ldc]
@@ -63,7 +65,26 @@ struct TcArgs {
     const float* bias;    // [N] or null
     float* sigsum;        // kEpiSigsum: out[N] += sum over rows of sigmoid
     int M, N, K, ldc;
+    int ksplit;           // kEpiF32Add: K slices per output tile, each adding its partial product into C
+    int kper;             // K tiles (of TK) per slice
 };
+
+// Work item w of a launch: output tile w % tiles, K slice w / tiles (K tiles
+// [kb, ke)).  The tiles run M fastest, so consecutive items reuse B slices.
+struct TcItem {
+    int m0, n0, kb, ke, slice;
+};
+
+__device__ __forceinline__ TcItem tc_item(const TcArgs& g, int w, int mt, int tiles, int ktiles) {
+    TcItem it;
+    const int t = w % tiles;
+    it.slice = w / tiles;
+    it.m0 = (t % mt) * TM;
+    it.n0 = (t / mt) * TN;
+    it.kb = it.slice * g.kper;
+    it.ke = min(ktiles, it.kb + g.kper);
+    return it;
+}
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -207,6 +228,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN, tiles = mt * nt;
     const int ktiles = g.K / TK;
+    const int items = tiles * g.ksplit;
     unsigned char* base = tc_smem + ((1024u - (smem_addr(tc_smem) & 1023u)) & 1023u);
     const uint32_t sA = smem_addr(base), sB = sA + STAGES * A_BYTES;
 
@@ -239,43 +261,44 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {
             // producer: TMA slices of A and B into the ring, tile after tile
             int it = 0;
-            for (int t = blockIdx.x; t < tiles && !*abort_v; t += gridDim.x) {
-                const int m0 = (t % mt) * TM, n0 = (t / mt) * TN;
-                int kt = 0;
-                for (; kt < ktiles; ++kt, ++it) {
+            for (int w = blockIdx.x; w < items && !*abort_v; w += gridDim.x) {
+                const TcItem c = tc_item(g, w, mt, tiles, ktiles);
+                int kt = c.kb;
+                for (; kt < c.ke; ++kt, ++it) {
                     const int s = it % STAGES;
                     if (it >= STAGES && !mbar_wait(smem_addr(&empty[s]), ((it / STAGES) - 1) & 1, abort_v)) break;
                     const uint32_t bar = smem_addr(&full[s]);
                     mbar_expect_tx(bar, STAGE_BYTES);
-                    tma_load_2d(sA + s * A_BYTES, &tmA, kt * TK, m0, bar);
-                    tma_load_2d(sB + s * B_BYTES, &tmB, kt * TK, n0, bar);
+                    tma_load_2d(sA + s * A_BYTES, &tmA, kt * TK, c.m0, bar);
+                    tma_load_2d(sB + s * B_BYTES, &tmB, kt * TK, c.n0, bar);
                     issued = it + 1;
                 }
-                if (kt < ktiles) break;
+                if (kt < c.ke) break;
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer: tile tl of this CTA accumulates in buffer tl & 1
             int it = 0, tl = 0;
-            for (int t = blockIdx.x; t < tiles && !*abort_v; t += gridDim.x, ++tl) {
+            for (int w = blockIdx.x; w < items && !*abort_v; w += gridDim.x, ++tl) {
+                const TcItem c = tc_item(g, w, mt, tiles, ktiles);
                 const int b = tl & 1, u = tl >> 1;
                 if (tl >= 2 && !mbar_wait(smem_addr(&acc_empty[b]), (u - 1) & 1, abort_v)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc = tmem + (uint32_t)(b * TN);
-                int kt = 0;
-                for (; kt < ktiles; ++kt, ++it) {
+                int kt = c.kb;
+                for (; kt < c.ke; ++kt, ++it) {
                     const int s = it % STAGES;
                     if (!mbar_wait(smem_addr(&full[s]), (it / STAGES) & 1, abort_v)) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint64_t ad = sw128_desc(sA + s * A_BYTES), bd = sw128_desc(sB + s * B_BYTES);
 #pragma unroll
                     for (int kk = 0; kk < TK / 16; ++kk)   // +32 bytes of K per MMA: +2 in the encoded address
-                        mma_bf16(acc, ad + 2 * kk, bd + 2 * kk, (kt | kk) != 0);
+                        mma_bf16(acc, ad + 2 * kk, bd + 2 * kk, (kt > c.kb || kk > 0) ? 1u : 0u);
                     mma_commit(smem_addr(&empty[s]));
                     consumed = it + 1;
                 }
-                if (kt < ktiles) break;
+                if (kt < c.ke) break;
                 mma_commit(smem_addr(&acc_full[b]));   // fires when the tile's MMAs have completed
             }
             if (*abort_v) {                          // let every MMA issued above land
@@ -288,14 +311,16 @@ __global__ void __launch_bounds__(THREADS, 1)
         // 32q .. 32q + 31), columns [cb, cb + 64) of the tile
         const int q = warp & 3, cb = ((warp - 2) >> 2) * 64;
         int tl = 0;
-        for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++tl) {
+        for (int w = blockIdx.x; w < items; w += gridDim.x, ++tl) {
             const int b = tl & 1, u = tl >> 1;
             int okw = 0;
             if (lane == 0) okw = mbar_wait(smem_addr(&acc_full[b]), u & 1, abort_v) ? 1 : 0;
             okw = __shfl_sync(0xffffffffu, okw, 0);      // warp-uniform (tcgen05.ld is warp-collective)
             if (!okw) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int m0 = (t % mt) * TM, n0 = (t / mt) * TN;
+            const TcItem ci = tc_item(g, w, mt, tiles, ktiles);
+            const int m0 = ci.m0, n0 = ci.n0;
+            const float* bias = ci.slice == 0 ? g.bias : nullptr;   // a split product adds the bias once
             const int row = m0 + q * 32 + lane;
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TN);
 #pragma unroll 1
@@ -305,9 +330,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const bool whole = nc + 16 <= g.N;
                 float v[16];
                 tmem_ld16(trow + c, v);
-                if (g.bias) {
+                if (bias) {
                     if (whole) {
-                        const float4* bp = reinterpret_cast<const float4*>(g.bias + nc);
+                        const float4* bp = reinterpret_cast<const float4*>(bias + nc);
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             const float4 bb = __ldg(bp + j);
@@ -316,7 +341,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     } else {
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
-                            if (nc + j < g.N) v[j] += __ldg(g.bias + nc + j);
+                            if (nc + j < g.N) v[j] += __ldg(bias + nc + j);
                     }
                 }
                 if (EPI == kEpiSigsum) {
@@ -328,7 +353,19 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if ((lane & 1) == 0 && col < g.N) atomicAdd(g.sigsum + col, sum);
                 } else if (row < g.M) {
                     const long long off = (long long)row * g.ldc + nc;
-                    if (EPI == kEpiF32) {
+                    if (EPI == kEpiF32Add) {
+                        float* Cp = reinterpret_cast<float*>(g.C) + off;
+                        if (whole) {
+#pragma unroll
+                            for (int j = 0; j < 16; j += 4)
+                                atomicAdd(reinterpret_cast<float4*>(Cp + j), make_float4(v[j], v[j + 1], v[j + 2],
+                                                                                         v[j + 3]));
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 16; ++j)
+                                if (nc + j < g.N) atomicAdd(Cp + j, v[j]);
+                        }
+                    } else if (EPI == kEpiF32) {
                         float* Cp = reinterpret_cast<float*>(g.C) + off;
                         if (whole) {
 #pragma unroll
@@ -433,12 +470,15 @@ bool make_map(CUtensorMap* map, const void* ptr, int rows, int k, int ld, int bo
 // Whether the tensor-core path takes this GEMM: K-major A and B, K a
 // multiple of 64, no split-K.
 bool gemm_tc_eligible(int a_kmajor, int b_kmajor, int K, int splitk) {
-    return a_kmajor && b_kmajor && K % TK == 0 && K > 0 && splitk <= 1 && encode_fn() != nullptr;
+    (void)splitk;
+    return a_kmajor && b_kmajor && K % TK == 0 && K > 0 && encode_fn() != nullptr;
 }
 
-// epi: 0 FP32 C, 1 GELU (C = H bf16, Z bf16), 2 sigmoid column sums into sigsum.
+// epi: 0 FP32 C, 1 GELU (C = H bf16, Z bf16), 2 sigmoid column sums into
+// sigsum; splitk > 1 (FP32 C only): K is cut into splitk slices whose partial
+// products are added into C, which the caller has zeroed.
 cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int epi, const float* bias,
-                           void* Z, float* sigsum, int M, int N, int K, cudaStream_t s) {
+                           void* Z, float* sigsum, int M, int N, int K, int splitk, cudaStream_t s) {
     CUtensorMap ta, tb;
     if (!make_map(&ta, A, M, K, lda, TM) || !make_map(&tb, B, N, K, ldb, TN)) return cudaErrorInvalidValue;
     TcArgs g;
@@ -447,8 +487,14 @@ cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void*
     g.bias = bias;
     g.sigsum = sigsum;
     g.M = M; g.N = N; g.K = K; g.ldc = ldc;
-    const int tiles = ((N + TN - 1) / TN) * ((M + TM - 1) / TM);
-    dim3 grid(tiles < sm_count() ? tiles : sm_count());
+    const int ktiles = K / TK;
+    if (splitk < 1 || epi != kEpiF32) splitk = 1;
+    if (splitk > ktiles) splitk = ktiles;
+    g.kper = (ktiles + splitk - 1) / splitk;
+    g.ksplit = (ktiles + g.kper - 1) / g.kper;        // no empty slice
+    if (g.ksplit > 1) epi = kEpiF32Add;
+    const int items = ((N + TN - 1) / TN) * ((M + TM - 1) / TM) * g.ksplit;
+    dim3 grid(items < sm_count() ? items : sm_count());
 #define ONEKA_TC_CASE(E)                                                                                    \
     {                                                                                                       \
         cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
@@ -457,6 +503,7 @@ cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void*
         gemm_tc_kernel<E><<<grid, THREADS, SMEM_BYTES, s>>>(ta, tb, g);                                     \
     }
     if (epi == kEpiF32) ONEKA_TC_CASE(kEpiF32)
+    else if (epi == kEpiF32Add) ONEKA_TC_CASE(kEpiF32Add)
     else if (epi == kEpiGelu) ONEKA_TC_CASE(kEpiGelu)
     else ONEKA_TC_CASE(kEpiSigsum)
 #undef ONEKA_TC_CASE

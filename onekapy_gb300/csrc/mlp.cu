@@ -264,9 +264,17 @@ __global__ void colsum_kernel(const __nv_bfloat16* __restrict__ x, int rows, int
 
 // AdamW with bias correction (decoupled weight decay), FP32 master weights,
 // and the BF16 copy the GEMMs read.
+// hyper (optional, device [3]): lr, 1 - b1^t, 1 - b2^t of this step, read on
+// the device so that a captured training step takes its schedule from memory.
 __global__ void adamw_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                              const float* __restrict__ g, __nv_bfloat16* __restrict__ wb, long long n, float lr,
-                             float b1, float b2, float eps, float wd, float c1, float c2) {
+                             float b1, float b2, float eps, float wd, float c1, float c2,
+                             const float* __restrict__ hyper) {
+    if (hyper) {
+        lr = hyper[0];
+        c1 = hyper[1];
+        c2 = hyper[2];
+    }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const float gi = g[i];
@@ -309,6 +317,49 @@ __global__ void sigmoid_colsum_kernel(const float* __restrict__ logits, int rows
     out[c] += s;
 }
 
+// dst[c][r] = src[r][c] for BF16 matrices: 64 x 64 tiles staged in shared
+// memory (rows padded by 16 bytes), 16-byte loads and stores, 256 threads.
+constexpr int TT = 64;
+__global__ void __launch_bounds__(256) transpose_bf16_kernel(const uint16_t* __restrict__ src, int rows, int cols,
+                                                             long long lds, uint16_t* __restrict__ dst, long long ldd) {
+    __shared__ __align__(16) uint16_t tile[TT][TT + 8];
+    const int r0 = blockIdx.y * TT, c0 = blockIdx.x * TT;
+    const int t = threadIdx.x;
+    // load: 64 rows x 8 chunks of 8 elements
+    for (int i = t; i < TT * (TT / 8); i += 256) {
+        const int r = i >> 3, ch = (i & 7) * 8;
+        const int gr = r0 + r, gc = c0 + ch;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (gr < rows) {
+            if (gc + 8 <= cols && (((uintptr_t)(src + gr * lds + gc)) & 15) == 0) {
+                v = *reinterpret_cast<const uint4*>(src + gr * lds + gc);
+            } else {
+                uint16_t e[8];
+                for (int j = 0; j < 8; ++j) e[j] = gc + j < cols ? src[gr * lds + gc + j] : 0;
+                v = make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16), e[6] | (e[7] << 16));
+            }
+        }
+        *reinterpret_cast<uint4*>(&tile[r][ch]) = v;
+    }
+    __syncthreads();
+    // store: output row c (a column of the tile), 8 chunks of 8 source rows
+    for (int i = t; i < TT * (TT / 8); i += 256) {
+        const int c = i >> 3, ch = (i & 7) * 8;
+        const int gc = c0 + c, gr = r0 + ch;
+        if (gc >= cols) continue;
+        uint16_t e[8];
+        for (int j = 0; j < 8; ++j) e[j] = tile[ch + j][c];
+        uint16_t* out = dst + gc * ldd + gr;
+        if (gr + 8 <= rows && (((uintptr_t)out) & 15) == 0) {
+            *reinterpret_cast<uint4*>(out) =
+                make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16), e[6] | (e[7] << 16));
+        } else {
+            for (int j = 0; j < 8; ++j)
+                if (gr + j < rows) out[j] = e[j];
+        }
+    }
+}
+
 unsigned grid_for(long long n, int per) {
     long long b = (n + per - 1) / per;
     return (unsigned)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
@@ -318,17 +369,17 @@ unsigned grid_for(long long n, int per) {
 
 bool gemm_tc_eligible(int a_kmajor, int b_kmajor, int K, int splitk);
 cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int epi, const float* bias,
-                           void* Z, float* sigsum, int M, int N, int K, cudaStream_t s);
+                           void* Z, float* sigsum, int M, int N, int K, int splitk, cudaStream_t s);
 
 // Which kernel a GEMM runs on: 1 the tcgen05 kernel (gemm_tc.cu), 0 the
 // mma.sync kernel below.  The tcgen05 kernel takes K-major operands with K a
-// multiple of 64 and no split-K, for the FP32, GELU and sigmoid-sum
+// multiple of 64, for the FP32 (also split-K), GELU and sigmoid-sum
 // epilogues; bit 0 of `flags` forces the mma.sync kernel.
 int gemm_path(int a_kmajor, int b_kmajor, int K, int splitk, int c_f32, int gelu, void* Z, float* sigsum, int flags) {
     if (flags & 1) return 0;
     if (!gemm_tc_eligible(a_kmajor, b_kmajor, K, splitk)) return 0;
-    if (sigsum) return 1;
-    if (gelu) return (!c_f32 && Z) ? 1 : 0;
+    if (sigsum) return splitk <= 1 ? 1 : 0;
+    if (gelu) return (!c_f32 && Z && splitk <= 1) ? 1 : 0;
     return c_f32 ? 1 : 0;
 }
 
@@ -336,7 +387,8 @@ cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B
                              int ldc, int c_f32, const float* bias, int gelu, void* Z, int M, int N, int K,
                              int splitk, float* sigsum, int flags, cudaStream_t s) {
     if (gemm_path(a_kmajor, b_kmajor, K, splitk, c_f32, gelu, Z, sigsum, flags))
-        return launch_gemm_tc(A, lda, B, ldb, C, ldc, sigsum ? 2 : (gelu ? 1 : 0), bias, Z, sigsum, M, N, K, s);
+        return launch_gemm_tc(A, lda, B, ldb, C, ldc, sigsum ? 2 : (gelu ? 1 : 0), bias, Z, sigsum, M, N, K, splitk,
+                              s);
     GemmArgs g;
     g.A = (const __nv_bfloat16*)A;
     g.B = (const __nv_bfloat16*)B;
@@ -390,7 +442,23 @@ cudaError_t launch_colsum(const void* x, int rows, int cols, float* out, cudaStr
 cudaError_t launch_adamw(float* w, float* m, float* v, const float* g, void* wb, long long n, float lr, float b1,
                          float b2, float eps, float wd, int step, cudaStream_t s) {
     const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-    adamw_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, m, v, g, (__nv_bfloat16*)wb, n, lr, b1, b2, eps, wd, c1, c2);
+    adamw_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, m, v, g, (__nv_bfloat16*)wb, n, lr, b1, b2, eps, wd, c1, c2,
+                                                   nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adamw_scheduled(float* w, float* m, float* v, const float* g, void* wb, long long n,
+                                   const float* hyper, float b1, float b2, float eps, float wd, cudaStream_t s) {
+    adamw_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, m, v, g, (__nv_bfloat16*)wb, n, 0.0f, b1, b2, eps, wd, 1.0f,
+                                                   1.0f, hyper);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_bf16(const void* src, int rows, int cols, long long lds, void* dst, long long ldd,
+                                  cudaStream_t s) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((cols + TT - 1) / TT), (unsigned)((rows + TT - 1) / TT));
+    transpose_bf16_kernel<<<grid, 256, 0, s>>>((const uint16_t*)src, rows, cols, lds, (uint16_t*)dst, ldd);
     return cudaGetLastError();
 }
 

@@ -748,7 +748,8 @@ cudaError_t launch_mode(const TrackLaunch& L, cudaStream_t s) {
     const int block = L.opts.block > 0 ? L.opts.block : 256;
     const int occ = L.opts.occupancy;
     if (block == 64) return launch_variant<MODE, 64, 8>(L, s);
-    if (block == 256) return occ >= 3 ? launch_variant<MODE, 256, 3>(L, s)
+    if (block == 256) return occ >= 4 ? launch_variant<MODE, 256, 4>(L, s)
+                           : occ >= 3 ? launch_variant<MODE, 256, 3>(L, s)
                                       : launch_variant<MODE, 256, 2>(L, s);
     if (block == 32) return launch_variant<MODE, 32, 16>(L, s);
     if (occ >= 8) return launch_variant<MODE, 128, 8>(L, s);
@@ -803,7 +804,8 @@ cudaError_t launch_track32_batch(const JobTable& T, int rows, cudaStream_t s) {
         if (need > smem) smem = need;
     }
     if (block == 64) return launch_batch_variant<64, 8>(T, rows, smem, s);
-    if (block == 256) return occ >= 3 ? launch_batch_variant<256, 3>(T, rows, smem, s)
+    if (block == 256) return occ >= 4 ? launch_batch_variant<256, 4>(T, rows, smem, s)
+                           : occ >= 3 ? launch_batch_variant<256, 3>(T, rows, smem, s)
                                       : launch_batch_variant<256, 2>(T, rows, smem, s);
     if (block == 32) return launch_batch_variant<32, 16>(T, rows, smem, s);
     if (occ >= 8) return launch_batch_variant<128, 8>(T, rows, smem, s);

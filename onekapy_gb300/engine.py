@@ -385,7 +385,8 @@ def track(site: Site, real: Realizations, release, opts: TrackOptions, grid: Gri
 # ---------------------------------------------------------------------------
 # autotuner: block shape, occupancy and chronicle window of the FP32 tracker
 # ---------------------------------------------------------------------------
-TUNE_CANDIDATES = [(256, 2, 32), (256, 3, 32), (128, 4, 32), (128, 6, 16), (128, 6, 32), (64, 8, 16)]
+TUNE_CANDIDATES = [(256, 2, 32), (256, 3, 32), (256, 4, 32), (256, 4, 16), (128, 4, 32), (128, 6, 16),
+                   (128, 6, 32), (128, 8, 16), (64, 8, 16)]
 _tuned: dict = {}
 
 

@@ -6,7 +6,8 @@ per-cell capture logits on the site grid.  It is trained in BF16 with FP32
 master weights on (parameters -> visited-cell mask) pairs that the tracker
 itself chronicles (oneka_track mark-only mode: one bitmask per realization),
 with the project's own kernels: oneka_gemm_bf16 (tensor cores),
-oneka_bce_bitmask, oneka_gelu_backward, oneka_colsum_bf16, oneka_adamw.
+oneka_transpose_bf16, oneka_bce_bitmask, oneka_gelu_backward,
+oneka_colsum_bf16, oneka_adamw.
 
 Screening: the surrogate's field is the mean of sigmoid(logits) over the
 screened realizations; a held-out fraction (the judges) is always tracked,
@@ -39,6 +40,7 @@ def _p(t):
 # flags of oneka_gemm_bf16: bit 0 forces the mma.sync kernel (default: the
 # tcgen05 kernel wherever it applies).
 GEMM_FLAGS = 0
+SM_COUNT = 152          # split-K targets about two work items per SM of a GB300
 
 
 def gemm(A, a_kmajor, B, b_kmajor, C_out, M, N, K, *, bias=None, gelu=False, Z=None, splitk=1, stream=None,
@@ -129,33 +131,57 @@ class MLP:
         """BCE against chronicle bitmasks (rows of slot_words words) and dlogits."""
         a = self._buffers(self._X.shape[0], self._X.device)
         B, ncells = a["logits"].shape
-        loss = torch.zeros(1, dtype=F32, device=self._X.device)
+        if "loss" not in a:
+            a["loss"] = torch.zeros(1, dtype=F32, device=self._X.device)
+        loss = a["loss"]
+        loss.zero_()
         C.check(C.load().oneka_bce_bitmask(_p(a["logits"]), _p(masks), slot_words, wpr, ncols, B, ncells,
                                            1.0 / (B * ncells), _p(a["dlogits"]), _p(loss), C.stream_ptr()))
         return loss
 
+    def _transposed(self, name, rows, cols, device):
+        key = ("T", name, rows, cols)
+        if key not in self._acts:
+            self._acts[key] = torch.empty((cols, rows), dtype=BF16, device=device)
+        return self._acts[key]
+
     def backward(self):
+        """Gradients of every layer.  The two GEMMs per layer contract over the
+        batch (gW = dZ^T H_in) and over the layer's outputs (dH_in = dZ W);
+        their operands are stored with the contracted index outermost, so they
+        are first transposed (oneka_transpose_bf16, bandwidth-bound) and both
+        GEMMs then run K-major on the tensor cores; dH_in, whose K is the
+        65,536 outputs of the last layer, is split over K."""
         X = self._X
         B = X.shape[0]
-        a = self._buffers(B, X.device)
+        dev = X.device
+        a = self._buffers(B, dev)
         n = len(self.layers)
+        Lb = C.load()
         dcur = a["dlogits"]                    # BF16 dZ of the current layer
         for i in range(n - 1, -1, -1):
             L = self.layers[i]
             dout, din = L.w.shape
             hin = X if i == 0 else a["H"][i - 1]
-            # gW = dZ^T H_in : [dout][din] = (dZ [B][dout])^T (H_in [B][din])
-            gemm(dcur, False, hin, False, L.gw, dout, din, B)
-            C.check(C.load().oneka_colsum_bf16(_p(dcur), B, dout, _p(L.gb), C.stream_ptr()))
+            # gW = dZ^T H_in : [dout][din] = (dZ^T [dout][B]) (H_in^T [din][B])^T
+            dzt = self._transposed(("dz", i), B, dout, dev)
+            hint = self._transposed(("h", i), B, din, dev)
+            C.check(Lb.oneka_transpose_bf16(_p(dcur), B, dout, dcur.shape[-1], _p(dzt), B, C.stream_ptr()))
+            C.check(Lb.oneka_transpose_bf16(_p(hin), B, din, hin.shape[-1], _p(hint), B, C.stream_ptr()))
+            gemm(dzt, True, hint, True, L.gw, dout, din, B)
+            C.check(Lb.oneka_colsum_bf16(_p(dcur), B, dout, _p(L.gb), C.stream_ptr()))
             if i == 0:
                 break
-            # dH_in = dZ W : [B][din], split over the long K = dout
+            # dH_in = dZ W : [B][din] = (dZ [B][dout]) (W^T [din][dout])^T, split over K = dout
+            wt = self._transposed(("w", i), dout, din, dev)
+            C.check(Lb.oneka_transpose_bf16(_p(L.wb), dout, din, din, _p(wt), dout, C.stream_ptr()))
             dh = a["dh"][i - 1]
             dh.zero_()
-            splitk = max(1, min(32, dout // 2048))
-            gemm(dcur, True, L.wb, False, dh, B, din, dout, splitk=splitk)
+            tiles = -(-B // 128) * -(-din // 256)
+            splitk = max(1, min(dout // 64, round(2 * SM_COUNT / tiles)))
+            gemm(dcur, True, wt, True, dh, B, din, dout, splitk=splitk)
             dz = a["dz"][i - 1]
-            C.check(C.load().oneka_gelu_backward(_p(dh), _p(a["Z"][i - 1]), _p(dz), dh.numel(), C.stream_ptr()))
+            C.check(Lb.oneka_gelu_backward(_p(dh), _p(a["Z"][i - 1]), _p(dz), dh.numel(), C.stream_ptr()))
             dcur = dz
 
     def adamw(self, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, weight_decay=1e-4):
@@ -166,6 +192,16 @@ class MLP:
                                    betas[1], eps, weight_decay, self.step_count, C.stream_ptr()))
             C.check(Lb.oneka_adamw(_p(L.b), _p(L.mb), _p(L.vb), _p(L.gb), None, L.b.numel(), lr, betas[0],
                                    betas[1], eps, 0.0, self.step_count, C.stream_ptr()))
+
+    def adamw_scheduled(self, hyper, betas=(0.9, 0.999), eps=1e-8, weight_decay=1e-4):
+        """AdamW with the step's lr and bias corrections read from the device
+        tensor hyper = [lr, 1 - beta1^t, 1 - beta2^t] (a captured step)."""
+        Lb = C.load()
+        for L in self.layers:
+            C.check(Lb.oneka_adamw_scheduled(_p(L.w), _p(L.mw), _p(L.vw), _p(L.gw), _p(L.wb), L.w.numel(),
+                                             _p(hyper), betas[0], betas[1], eps, weight_decay, C.stream_ptr()))
+            C.check(Lb.oneka_adamw_scheduled(_p(L.b), _p(L.mb), _p(L.vb), _p(L.gb), None, L.b.numel(), _p(hyper),
+                                             betas[0], betas[1], eps, 0.0, C.stream_ptr()))
 
     def sigmoid_sum(self, X, out):
         """out[c] += sum over rows of sigmoid(logits) (the screened visits);
@@ -264,25 +300,54 @@ def screen(model: MLP, feats: Features, site: E.Site, real: E.Realizations, rele
 
 
 def train(model: MLP, X: torch.Tensor, masks: torch.Tensor, slot_words: int, wpr: int, ncols: int, *,
-          epochs=3, batch=512, lr=1e-3, weight_decay=1e-4, lr_final=1e-4, log=None):
-    """Mini-batch AdamW over consecutive batches (realizations are i.i.d. draws)."""
+          epochs=3, batch=512, lr=1e-3, weight_decay=1e-4, lr_final=1e-4, log=None, graph=True):
+    """Mini-batch AdamW over consecutive batches (realizations are i.i.d. draws).
+
+    With `graph` the training step (forward, loss, backward, AdamW: about 40
+    kernel launches) is captured once as a CUDA graph after one eager step
+    and replayed for every later batch; each batch is first copied into the
+    graph's fixed input buffers, and the step's learning rate and bias
+    corrections into a device tensor that the AdamW kernels read."""
     n = X.shape[0]
     nb = n // batch
     total = epochs * nb
+    betas, eps = (0.9, 0.999), 1e-8
+    dev = X.device
+    xs = torch.empty((batch, X.shape[1]), dtype=X.dtype, device=dev)
+    ms = torch.empty((batch, masks.shape[1]), dtype=masks.dtype, device=dev)
+    hyper = torch.zeros(3, dtype=F32, device=dev)
+
+    def body():
+        model.forward(xs)
+        model.loss_and_grad(ms, slot_words, wpr, ncols)
+        model.backward()
+        model.adamw_scheduled(hyper, betas, eps, weight_decay)
+
+    g = None
     losses = []
     for ep in range(epochs):
         for k in range(nb):
             step = ep * nb + k
             frac = step / max(1, total - 1)
             lr_k = lr * (lr_final / lr) ** frac          # exponential decay to lr_final
-            xb = X[k * batch:(k + 1) * batch]
-            mb = masks[k * batch:(k + 1) * batch]
-            model.forward(xb)
-            loss = model.loss_and_grad(mb, slot_words, wpr, ncols)
-            model.backward()
-            model.adamw(lr=lr_k, weight_decay=weight_decay)
+            model.step_count += 1
+            t = model.step_count
+            xs.copy_(X[k * batch:(k + 1) * batch], non_blocking=True)
+            ms.copy_(masks[k * batch:(k + 1) * batch], non_blocking=True)
+            hyper.copy_(torch.tensor([lr_k, 1.0 - betas[0] ** t, 1.0 - betas[1] ** t], dtype=F32).pin_memory(),
+                        non_blocking=True)
+            if not graph:
+                body()
+            elif g is None:
+                body()                                   # one eager step: buffers, kernels and maps set up
+                torch.cuda.synchronize()
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    body()
+            else:
+                g.replay()
             if k % 50 == 0 or k == nb - 1:
-                losses.append(float(loss.item()))
+                losses.append(float(model._buffers(batch, dev)["loss"].item()))
                 if log:
                     log(ep, k, losses[-1])
     return losses

@@ -17,7 +17,7 @@ from onekapy_gb300 import surrogate as SG  # noqa: E402
 @pytest.mark.parametrize("flags", [0, 1])
 @pytest.mark.parametrize("a_kmajor,b_kmajor", [(True, True), (True, False), (False, True), (False, False)])
 @pytest.mark.parametrize("M,N,K,splitk", [(256, 384, 96, 1), (200, 72, 64, 1), (128, 512, 1024, 8),
-                                          (296, 520, 512, 1), (64, 65536, 512, 1)])
+                                          (296, 520, 512, 1), (64, 65536, 512, 1), (512, 512, 65536, 37)])
 def test_gemm_layouts_match_fp32(flags, a_kmajor, b_kmajor, M, N, K, splitk):
     """Both GEMM kernels (tcgen05 where it applies, and the forced mma.sync
     kernel) against an FP32 product of the same BF16 operands."""
@@ -34,9 +34,22 @@ def test_gemm_layouts_match_fp32(flags, a_kmajor, b_kmajor, M, N, K, splitk):
     if bias is not None:
         ref = ref + bias
     tc = SG.gemm_path(a_kmajor, b_kmajor, K, splitk=splitk, flags=flags)
-    assert tc == int(flags == 0 and a_kmajor and b_kmajor and K % 64 == 0 and splitk == 1)
+    assert tc == int(flags == 0 and a_kmajor and b_kmajor and K % 64 == 0)
     assert SG.tc_status() == 0
     assert torch.allclose(Cf, ref, rtol=1e-3, atol=1e-3 * math.sqrt(K)), float((Cf - ref).abs().max())
+
+
+@pytest.mark.parametrize("rows,cols,lds,ldd", [(512, 65536, 65536, 512), (96, 200, 208, 104), (7, 13, 16, 8),
+                                               (130, 64, 64, 136)])
+def test_transpose_bf16(rows, cols, lds, ldd):
+    """oneka_transpose_bf16 against torch's transpose, padded leading dimensions untouched."""
+    dev = C.device()
+    src = torch.randn((rows, lds), device=dev).to(torch.bfloat16)
+    dst = torch.full((cols, ldd), 7.0, dtype=torch.bfloat16, device=dev)
+    C.check(C.load().oneka_transpose_bf16(C.ptr(src), rows, cols, lds, C.ptr(dst), ldd, C.stream_ptr()))
+    torch.cuda.synchronize()
+    assert torch.equal(dst[:, :rows], src[:, :cols].T)
+    assert bool((dst[:, rows:] == 7.0).all())
 
 
 @pytest.mark.parametrize("flags", [0, 1])
@@ -85,6 +98,30 @@ def test_mlp_gradients_match_cpu_oracle():
         assert np.linalg.norm(gb - db[i]) <= 0.03 * np.linalg.norm(db[i]) + 1e-12, i
 
 
+def test_graph_captured_training_matches_eager():
+    """SG.train with the training step captured as a CUDA graph (and its
+    schedule read from the device by oneka_adamw_scheduled) follows the
+    eager loop: same losses and weights up to the order of the split-K
+    atomic sums."""
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(5)
+    X = (torch.randn((2048, 64), generator=g) * 0.8).to(dev).to(torch.bfloat16)
+    bits = torch.rand((2048, 64, 64), generator=g) < 0.2
+    words = (bits.reshape(2048, 64, 2, 32).to(torch.int64) << torch.arange(32)).sum(-1)
+    masks = torch.where(words >= 2**31, words - 2**32, words).to(torch.int32).reshape(2048, 128).to(dev)
+    runs = {}
+    for graph in (False, True):
+        model = SG.MLP([64, 256, 256, 4096], dev, seed=2, out_bias=-1.0)
+        losses = SG.train(model, X, masks, 128, 2, 64, epochs=2, batch=256, lr=2e-3, lr_final=5e-4, graph=graph)
+        torch.cuda.synchronize()
+        runs[graph] = (losses, [L.w.clone() for L in model.layers])
+    (l0, w0), (l1, w1) = runs[False], runs[True]
+    assert len(l0) == len(l1) and l0[-1] < l0[0]
+    assert np.allclose(l0, l1, rtol=1e-3, atol=1e-6), (l0, l1)
+    for a, b in zip(w0, w1):
+        assert float((a - b).norm() / a.norm()) < 1e-3
+
+
 def test_adamw_matches_restatement():
     import mlp_oracle
     dev = C.device()
@@ -122,10 +159,12 @@ def test_fused_sigmoid_colsum_matches_fp32(flags):
 
 def test_trained_surrogate_screens_faster_within_tolerance():
     """Train on tracker-chronicled masks of the 31-well site (1000 paths, 20
-    years, a 128 x 128 grid at 20 m, 8 k realizations), then screen 8 k
-    fresh realizations with 5 % judges: the judges accept the surrogate, the
-    screened field agrees with tracking every realization, and screening
-    costs less than tracking everything."""
+    years, a 128 x 128 grid at 20 m, 64 k realizations), then screen 16 k
+    fresh realizations with 25 % judges: the judges accept the surrogate at
+    the tracker's own bar (L-inf <= 0.01), the screened field agrees with
+    tracking every realization, and screening costs less than tracking
+    everything.  (The judges' L-inf includes their sampling noise, about
+    sqrt(p (1 - p) / n) per cell, hence 4,096 judges.)"""
     dev = C.device()
     spec = S.config5(npaths=1000)
     site = E.Site(spec.wells, spec.observations, spec.base, c_dist=spec.c_dist, p_dist=spec.p_dist,
@@ -135,18 +174,19 @@ def test_trained_surrogate_screens_faster_within_tolerance():
     release = torch.as_tensor(site.release(spec.npaths), device=dev)
     opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
                           confined=False, precision=C.FP32)
-    train_real = E.realize(site, 8192, seed=77)
+    train_real = E.realize(site, 65536, seed=77)
     masks, slot_words = SG.chronicle_masks(site, train_real, release, opts, grid)
     feats = SG.Features(train_real, site.nwells)
     X = feats(train_real)
-    model = SG.MLP([64, 256, 256, 256, nr * nc], dev, seed=3, out_bias=math.log(0.05 / 0.95))
-    losses = SG.train(model, X, masks, slot_words, grid.words_per_row, nc, epochs=4, batch=256, lr=2e-3,
-                      lr_final=2e-4)
+    model = SG.MLP([64, 512, 512, 512, nr * nc], dev, seed=3, out_bias=math.log(0.05 / 0.95))
+    losses = SG.train(model, X, masks, slot_words, grid.words_per_row, nc, epochs=8, batch=512, lr=1.5e-3,
+                      lr_final=1e-4)
     assert losses[-1] < 0.5 * losses[0], losses
-    fresh = E.realize(site, 8192, seed=78)
-    SG.screen(model, feats, site, fresh.slice(0, 1024), release, opts, grid, judge_fraction=0.05,
+    fresh = E.realize(site, 16384, seed=78)
+    SG.screen(model, feats, site, fresh.slice(0, 1024), release, opts, grid, judge_fraction=0.25,
               tolerance=1.0)                                   # warm-up
-    res = SG.screen(model, feats, site, fresh, release, opts, grid, judge_fraction=0.05, tolerance=0.1)
+    # the acceptance bar is the FP32 tracker's own: L-inf <= 0.01 over the judges
+    res = SG.screen(model, feats, site, fresh, release, opts, grid, judge_fraction=0.25, tolerance=0.01)
     assert res.accepted, (res.judge_linf, res.judge_l1)
     counts = torch.zeros((nr, nc), dtype=torch.int32, device=dev)
     E.track(site, fresh.slice(0, 1024), release, opts, grid, counts=counts)   # warm-up
@@ -165,7 +205,7 @@ def test_trained_surrogate_screens_faster_within_tolerance():
           f"{float(err.max()):.4f} L1 {float(err.mean()):.2e}; screen {res.seconds * 1e3:.1f} ms "
           f"(judges {res.seconds_judges * 1e3:.1f}, surrogate {res.seconds_surrogate * 1e3:.1f}) vs "
           f"track-all {t_track * 1e3:.1f} ms")
-    assert float(err.max()) < 0.1
+    assert float(err.max()) < 0.02
     assert res.seconds < t_track, (res.seconds, t_track)
 
 
@@ -184,8 +224,8 @@ def test_untrained_surrogate_is_rejected_and_every_realization_tracked():
     real = E.realize(site, 600, seed=21)
     feats = SG.Features(real, site.nwells)
     model = SG.MLP([64, 64, 64, 64 * 64], dev, seed=1, out_bias=2.0)      # sigmoid(2) = 0.88 everywhere
-    res = SG.screen(model, feats, site, real, release, opts, grid, judge_fraction=0.05, tolerance=0.05)
-    assert not res.accepted and res.judge_linf > 0.05
+    res = SG.screen(model, feats, site, real, release, opts, grid, judge_fraction=0.05, tolerance=0.01)
+    assert not res.accepted and res.judge_linf > 0.01
     counts = torch.zeros((64, 64), dtype=torch.int32, device=dev)
     E.track(site, real, release, opts, grid, counts=counts)
     assert torch.equal(res.field, counts.double().reshape(64, 64) / real.n)
