@@ -427,6 +427,25 @@ ONEKA_API int oneka_adamw_scheduled(float* w, float* m, float* v, const float* g
                                     const float* hyper, float beta1, float beta2, float eps, float weight_decay,
                                     void* stream);
 
+/*
+ * oneka_bce_bitmask that also writes the gradient transposed, dlogits_t
+ * [ncells][ldt] (BF16), for the weight-gradient GEMM's K-major operand.
+ * ncols and B multiples of 64, ldt a multiple of 8 and >= B.
+ */
+ONEKA_API int oneka_bce_bitmask_t(const float* logits, const uint32_t* masks, int64_t slot_words, int32_t wpr,
+                                  int32_t ncols, int32_t B, int32_t ncells, float scale, void* dlogits,
+                                  void* dlogits_t, int64_t ldt, float* loss, void* stream);
+
+/*
+ * oneka_adamw_scheduled for a weight matrix w [rows][cols] that also writes
+ * the BF16 copy transposed, w_bf16_t [cols][ldt], for the backward pass's
+ * K-major operand.  rows and cols multiples of 64, ldt a multiple of 8 and
+ * >= rows.
+ */
+ONEKA_API int oneka_adamw_scheduled_t(float* w, float* m, float* v, const float* g, void* w_bf16, void* w_bf16_t,
+                                      int64_t ldt, int32_t rows, int32_t cols, const float* hyper, float beta1,
+                                      float beta2, float eps, float weight_decay, void* stream);
+
 /* Standardized BF16 features [n][ld] of realizations: A..F, discharges, K, porosity (nf = 8 + nwells). */
 ONEKA_API int oneka_features(const double* coef, const double* q, const double* aquifer, int32_t nwells,
                              int32_t n, const float* mean, const float* inv_std, int32_t nf, int32_t ld,

@@ -30,7 +30,7 @@ EXPORTS = ["oneka_abi_version", "oneka_last_error", "oneka_site_logr2", "oneka_r
            "oneka_gelu_backward", "oneka_colsum_bf16", "oneka_adamw", "oneka_features",
            "oneka_sigmoid_colsum", "oneka_gemm_bf16_sigmoid_colsum", "oneka_gemm_bf16_path",
            "oneka_gemm_tc_status", "oneka_fit_rows", "oneka_fit_solve", "oneka_transpose_bf16",
-           "oneka_adamw_scheduled"]
+           "oneka_adamw_scheduled", "oneka_bce_bitmask_t", "oneka_adamw_scheduled_t"]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 _P = ctypes.c_void_p
@@ -112,6 +112,12 @@ def load() -> ctypes.CDLL:
         L.oneka_adamw_scheduled.restype = ctypes.c_int
         L.oneka_adamw_scheduled.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int64, _P, ctypes.c_float, ctypes.c_float,
                                             ctypes.c_float, ctypes.c_float, _P]
+        L.oneka_bce_bitmask_t.restype = ctypes.c_int
+        L.oneka_bce_bitmask_t.argtypes = [_P, _P, ctypes.c_int64, _I, _I, _I, _I, ctypes.c_float, _P, _P,
+                                          ctypes.c_int64, _P, _P]
+        L.oneka_adamw_scheduled_t.restype = ctypes.c_int
+        L.oneka_adamw_scheduled_t.argtypes = [_P, _P, _P, _P, _P, _P, ctypes.c_int64, _I, _I, _P, ctypes.c_float,
+                                              ctypes.c_float, ctypes.c_float, ctypes.c_float, _P]
         L.oneka_transpose_bf16.restype = ctypes.c_int
         L.oneka_transpose_bf16.argtypes = [_P, _I, _I, ctypes.c_int64, _P, ctypes.c_int64, _P]
         L.oneka_fit_rows.restype = ctypes.c_int

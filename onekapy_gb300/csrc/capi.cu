@@ -48,6 +48,12 @@ cudaError_t launch_transpose_bf16(const void* src, int rows, int cols, long long
                                   cudaStream_t s);
 cudaError_t launch_adamw_scheduled(float* w, float* m, float* v, const float* g, void* wb, long long n,
                                    const float* hyper, float b1, float b2, float eps, float wd, cudaStream_t s);
+cudaError_t launch_bce_bitmask_t(const float* logits, const uint32_t* masks, long long slot_words, int wpr,
+                                 int ncols, int B, int ncells, float scale, void* dlogits, void* dlogits_t,
+                                 long long ldt, float* loss, cudaStream_t s);
+cudaError_t launch_adamw_t(float* w, float* m, float* v, const float* g, void* wb, void* wbt, long long ldt, int rows,
+                           int cols, const float* hyper, float b1, float b2, float eps, float wd, cudaStream_t s);
+
 cudaError_t launch_evaluate(const OnekaSite& site, const double* q, double K, double n, double H,
                             const double* coef, const double* pts, long long npts, int confined,
                             double* potential, double* discharge, double* head, double* velocity,
@@ -526,6 +532,32 @@ int oneka_adamw_scheduled(float* w, float* m, float* v, const float* g, void* w_
     ONEKA_CHECK_ARG(w && m && v && g && hyper && n >= 0, "adamw arguments");
     ONEKA_CHECK_CUDA(launch_adamw_scheduled(w, m, v, g, w_bf16, n, hyper, beta1, beta2, eps, weight_decay,
                                             (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_bce_bitmask_t(const float* logits, const uint32_t* masks, int64_t slot_words, int32_t wpr, int32_t ncols,
+                        int32_t B, int32_t ncells, float scale, void* dlogits, void* dlogits_t, int64_t ldt,
+                        float* loss, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(logits && masks && dlogits && dlogits_t && B > 0 && ncells > 0 && ncols > 0, "bce arguments");
+    ONEKA_CHECK_ARG(ncols % 64 == 0 && ncells % ncols == 0 && B % 64 == 0 && B <= 65535 * 64 && ldt % 8 == 0 &&
+                    ldt >= B, "ncols and B must be multiples of 64, ldt of 8 and >= B");
+    ONEKA_CHECK_ARG(al16(logits) && al16(dlogits) && al16(dlogits_t), "16-byte alignment");
+    ONEKA_CHECK_CUDA(launch_bce_bitmask_t(logits, masks, slot_words, wpr, ncols, B, ncells, scale, dlogits, dlogits_t,
+                                          ldt, loss, (cudaStream_t)stream));
+    return ONEKA_OK;
+}
+
+int oneka_adamw_scheduled_t(float* w, float* m, float* v, const float* g, void* w_bf16, void* w_bf16_t, int64_t ldt,
+                            int32_t rows, int32_t cols, const float* hyper, float beta1, float beta2, float eps,
+                            float weight_decay, void* stream) {
+    g_err[0] = 0;
+    ONEKA_CHECK_ARG(w && m && v && g && w_bf16 && w_bf16_t && hyper && rows > 0 && cols > 0, "adamw arguments");
+    ONEKA_CHECK_ARG(rows % 64 == 0 && cols % 64 == 0 && rows <= 65535 * 64 && ldt % 8 == 0 && ldt >= rows,
+                    "rows and cols must be multiples of 64, ldt of 8 and >= rows");
+    ONEKA_CHECK_ARG(al16(w) && al16(m) && al16(v) && al16(g) && al16(w_bf16) && al16(w_bf16_t), "16-byte alignment");
+    ONEKA_CHECK_CUDA(launch_adamw_t(w, m, v, g, w_bf16, w_bf16_t, ldt, rows, cols, hyper, beta1, beta2, eps,
+                                    weight_decay, (cudaStream_t)stream));
     return ONEKA_OK;
 }
 

@@ -225,6 +225,110 @@ __global__ void __launch_bounds__(THREADS) gemm_bf16_kernel(const GemmArgs g) {
 // Mean binary cross-entropy of logits z against the bits of a chronicle
 // mask (cell i*ncols + j <-> bit j%32 of word i*wpr + j/32 of the sample's
 // slot), and its gradient (sigmoid(z) - y) * scale as BF16.
+__device__ __forceinline__ float bce_term(float z, float y, float scale, float& grad) {
+    // max(z, 0) - z y + log(1 + e^-|z|) and d/dz = sigmoid(z) - y, with one exponential
+    const float e = __expf(-fabsf(z));
+    const float inv = __frcp_rn(1.0f + e);
+    const float p = z >= 0.0f ? inv : e * inv;
+    grad = (p - y) * scale;
+    return fmaxf(z, 0.0f) - z * y + __logf(1.0f + e);
+}
+
+// Eight consecutive cells of one grid row per thread: two float4 logit loads,
+// one mask word, one 16-byte store of BF16 gradients.  blockIdx.y is the
+// sample.  Needs ncols % 8 == 0 (else bce_bitmask_kernel below).
+__global__ void __launch_bounds__(256) bce_bitmask8_kernel(const float* __restrict__ logits,
+                                                           const uint32_t* __restrict__ masks, long long slot_words,
+                                                           int wpr, int ncols, int ncells, float scale,
+                                                           __nv_bfloat16* __restrict__ dlogits,
+                                                           float* __restrict__ loss) {
+    const int b = blockIdx.y;
+    const int chunk = blockIdx.x * blockDim.x + threadIdx.x;
+    float part = 0.0f;
+    if (chunk < ncells / 8) {
+        const int cell = chunk * 8, row = cell / ncols, col = cell - row * ncols;
+        const uint32_t w = masks[(long long)b * slot_words + (long long)row * wpr + (col >> 5)] >> (col & 31);
+        const long long i = (long long)b * ncells + cell;
+        const float4 z0 = *reinterpret_cast<const float4*>(logits + i);
+        const float4 z1 = *reinterpret_cast<const float4*>(logits + i + 4);
+        const float z[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+        float g[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) part += bce_term(z[j], (float)((w >> j) & 1u), scale, g[j]);
+        if (dlogits) {
+            uint32_t q[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(g[2 * j], g[2 * j + 1]);
+                q[j] = *reinterpret_cast<const uint32_t*>(&h);
+            }
+            *reinterpret_cast<uint4*>(dlogits + i) = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    __shared__ float wsum[8];
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0 && loss) {
+        float t = 0.0f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += wsum[k];
+        atomicAdd(loss, t * scale);
+    }
+}
+
+// BCE over a tile of 64 samples x 64 cells of one grid row, writing the
+// gradient both row-major (dlogits [B][ncells]) and transposed (dlogits_t
+// [ncells][ldt]), the latter through a shared-memory tile: the weight
+// gradient GEMM reads it K-major, so no separate transpose pass is needed.
+// Needs ncols % 64 == 0, B % 64 == 0, ldt % 8 == 0.
+__global__ void __launch_bounds__(256) bce_bitmask_t_kernel(const float* __restrict__ logits,
+                                                            const uint32_t* __restrict__ masks, long long slot_words,
+                                                            int wpr, int ncols, int ncells, float scale,
+                                                            __nv_bfloat16* __restrict__ dlogits,
+                                                            __nv_bfloat16* __restrict__ dlogits_t, long long ldt,
+                                                            float* __restrict__ loss) {
+    __shared__ __align__(16) __nv_bfloat16 tile[64][72];
+    __shared__ float wsum[8];
+    const int c0 = blockIdx.x * 64, b0 = blockIdx.y * 64;
+    const int grow = c0 / ncols, gcol0 = c0 - grow * ncols;
+    float part = 0.0f;
+    for (int i = threadIdx.x; i < 64 * 16; i += 256) {
+        const int r = i >> 4, q = (i & 15) * 4;
+        const int b = b0 + r, col = gcol0 + q;
+        const uint32_t w = masks[(long long)b * slot_words + (long long)grow * wpr + (col >> 5)] >> (col & 31);
+        const long long idx = (long long)b * ncells + c0 + q;
+        const float4 z = *reinterpret_cast<const float4*>(logits + idx);
+        const float zz[4] = {z.x, z.y, z.z, z.w};
+        float g[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) part += bce_term(zz[j], (float)((w >> j) & 1u), scale, g[j]);
+        const __nv_bfloat162 h0 = __floats2bfloat162_rn(g[0], g[1]), h1 = __floats2bfloat162_rn(g[2], g[3]);
+        const uint2 packed = make_uint2(*reinterpret_cast<const uint32_t*>(&h0),
+                                        *reinterpret_cast<const uint32_t*>(&h1));
+        *reinterpret_cast<uint2*>(dlogits + idx) = packed;
+        *reinterpret_cast<uint2*>(&tile[r][q]) = packed;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 64 * 8; i += 256) {
+        const int cc = i >> 3, s8 = (i & 7) * 8;
+        uint32_t e[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const __nv_bfloat162 h = __halves2bfloat162(tile[s8 + 2 * j][cc], tile[s8 + 2 * j + 1][cc]);
+            e[j] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(dlogits_t + (long long)(c0 + cc) * ldt + b0 + s8) = make_uint4(e[0], e[1], e[2], e[3]);
+    }
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0 && loss) {
+        float t = 0.0f;
+        for (int k = 0; k < 8; ++k) t += wsum[k];
+        atomicAdd(loss, t * scale);
+    }
+}
+
 __global__ void bce_bitmask_kernel(const float* __restrict__ logits, const uint32_t* __restrict__ masks,
                                    long long slot_words, int wpr, int ncols, int B, int ncells, float scale,
                                    __nv_bfloat16* __restrict__ dlogits, float* __restrict__ loss) {
@@ -235,11 +339,9 @@ __global__ void bce_bitmask_kernel(const float* __restrict__ logits, const uint3
         const int b = (int)(i / ncells), c = (int)(i % ncells);
         const int row = c / ncols, col = c % ncols;
         const uint32_t w = masks[(long long)b * slot_words + (long long)row * wpr + (col >> 5)];
-        const float y = (float)((w >> (col & 31)) & 1u);
-        const float z = logits[i];
-        part += fmaxf(z, 0.0f) - z * y + log1pf(expf(-fabsf(z)));
-        const float p = 1.0f / (1.0f + expf(-z));
-        if (dlogits) dlogits[i] = __float2bfloat16((p - y) * scale);
+        float g;
+        part += bce_term(logits[i], (float)((w >> (col & 31)) & 1u), scale, g);
+        if (dlogits) dlogits[i] = __float2bfloat16(g);
     }
     for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
     if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, part * scale);
@@ -253,13 +355,25 @@ __global__ void gelu_backward_kernel(const float* __restrict__ dh, const __nv_bf
         dz[i] = __float2bfloat16(dh[i] * gelu_grad(__bfloat162float(z[i])));
 }
 
-// out[c] = sum_r x[r][c] (bias gradients), x in BF16, one thread per column.
-__global__ void colsum_kernel(const __nv_bfloat16* __restrict__ x, int rows, int cols, float* __restrict__ out) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cols) return;
+// out[c] = sum_r x[r][c] (bias gradients), x in BF16: a block of 8 warps
+// per 32 columns, each warp a strided eighth of the rows, then a
+// shared-memory sum over the warps.
+__global__ void __launch_bounds__(256) colsum_kernel(const __nv_bfloat16* __restrict__ x, int rows, int cols,
+                                                     float* __restrict__ out) {
+    __shared__ float part[8][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * 32 + lane;
     float s = 0.0f;
-    for (int r = 0; r < rows; ++r) s += __bfloat162float(x[(long long)r * cols + c]);
-    out[c] = s;
+    if (c < cols)
+        for (int r = warp; r < rows; r += 8) s += __bfloat162float(x[(long long)r * cols + c]);
+    part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && c < cols) {
+        float t = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) t += part[k][lane];
+        out[c] = t;
+    }
 }
 
 // AdamW with bias correction (decoupled weight decay), FP32 master weights,
@@ -286,6 +400,61 @@ __global__ void adamw_kernel(float* __restrict__ w, float* __restrict__ m, float
         const float wi = w[i] - lr * (upd + wd * w[i]);
         w[i] = wi;
         if (wb) wb[i] = __float2bfloat16(wi);
+    }
+}
+
+// AdamW over a 64 x 64 tile of a [rows][cols] weight matrix (the update of
+// adamw_kernel, with the schedule in hyper), writing the BF16 copy both
+// row-major (wb) and transposed (wbt [cols][ldt]) through shared memory: the
+// backward pass reads W^T K-major, so no separate transpose pass is needed.
+// Needs cols % 64 == 0, rows % 64 == 0, ldt % 8 == 0.
+__global__ void __launch_bounds__(256) adamw_t_kernel(float* __restrict__ w, float* __restrict__ m,
+                                                      float* __restrict__ v, const float* __restrict__ g,
+                                                      __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbt,
+                                                      long long ldt, int cols, const float* __restrict__ hyper,
+                                                      float b1, float b2, float eps, float wd) {
+    __shared__ __align__(16) __nv_bfloat16 tile[64][72];
+    const float lr = hyper[0], c1 = hyper[1], c2 = hyper[2];
+    const int c0 = blockIdx.x * 64, r0 = blockIdx.y * 64;
+    for (int i = threadIdx.x; i < 64 * 16; i += 256) {
+        const int r = i >> 4, q = (i & 15) * 4;
+        const long long idx = (long long)(r0 + r) * cols + c0 + q;
+        float4 W = *reinterpret_cast<const float4*>(w + idx);
+        float4 M = *reinterpret_cast<const float4*>(m + idx);
+        float4 V = *reinterpret_cast<const float4*>(v + idx);
+        const float4 G = *reinterpret_cast<const float4*>(g + idx);
+        float* Wp = &W.x;
+        float* Mp = &M.x;
+        float* Vp = &V.x;
+        const float* Gp = &G.x;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float mi = b1 * Mp[j] + (1.0f - b1) * Gp[j];
+            const float vi = b2 * Vp[j] + (1.0f - b2) * Gp[j] * Gp[j];
+            Mp[j] = mi;
+            Vp[j] = vi;
+            const float upd = (mi / c1) / (sqrtf(vi / c2) + eps);
+            Wp[j] = Wp[j] - lr * (upd + wd * Wp[j]);
+        }
+        *reinterpret_cast<float4*>(w + idx) = W;
+        *reinterpret_cast<float4*>(m + idx) = M;
+        *reinterpret_cast<float4*>(v + idx) = V;
+        const __nv_bfloat162 h0 = __floats2bfloat162_rn(W.x, W.y), h1 = __floats2bfloat162_rn(W.z, W.w);
+        const uint2 packed = make_uint2(*reinterpret_cast<const uint32_t*>(&h0),
+                                        *reinterpret_cast<const uint32_t*>(&h1));
+        *reinterpret_cast<uint2*>(wb + idx) = packed;
+        *reinterpret_cast<uint2*>(&tile[r][q]) = packed;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 64 * 8; i += 256) {
+        const int cc = i >> 3, s8 = (i & 7) * 8;
+        uint32_t e[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const __nv_bfloat162 h = __halves2bfloat162(tile[s8 + 2 * j][cc], tile[s8 + 2 * j + 1][cc]);
+            e[j] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(wbt + (long long)(c0 + cc) * ldt + r0 + s8) = make_uint4(e[0], e[1], e[2], e[3]);
     }
 }
 
@@ -424,8 +593,15 @@ cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B
 
 cudaError_t launch_bce_bitmask(const float* logits, const uint32_t* masks, long long slot_words, int wpr, int ncols,
                                int B, int ncells, float scale, void* dlogits, float* loss, cudaStream_t s) {
-    bce_bitmask_kernel<<<grid_for((long long)B * ncells, 256), 256, 0, s>>>(
-        logits, masks, slot_words, wpr, ncols, B, ncells, scale, (__nv_bfloat16*)dlogits, loss);
+    const bool aligned = ((uintptr_t)logits & 15) == 0 && (!dlogits || ((uintptr_t)dlogits & 15) == 0);
+    if (ncols % 8 == 0 && aligned && B <= 65535) {
+        dim3 grid((unsigned)((ncells / 8 + 255) / 256), (unsigned)B);
+        bce_bitmask8_kernel<<<grid, 256, 0, s>>>(logits, masks, slot_words, wpr, ncols, ncells, scale,
+                                                 (__nv_bfloat16*)dlogits, loss);
+    } else {
+        bce_bitmask_kernel<<<grid_for((long long)B * ncells, 256), 256, 0, s>>>(
+            logits, masks, slot_words, wpr, ncols, B, ncells, scale, (__nv_bfloat16*)dlogits, loss);
+    }
     return cudaGetLastError();
 }
 
@@ -435,7 +611,7 @@ cudaError_t launch_gelu_backward(const float* dh, const void* z, void* dz, long 
 }
 
 cudaError_t launch_colsum(const void* x, int rows, int cols, float* out, cudaStream_t s) {
-    colsum_kernel<<<(cols + 255) / 256, 256, 0, s>>>((const __nv_bfloat16*)x, rows, cols, out);
+    colsum_kernel<<<(cols + 31) / 32, 256, 0, s>>>((const __nv_bfloat16*)x, rows, cols, out);
     return cudaGetLastError();
 }
 
@@ -451,6 +627,23 @@ cudaError_t launch_adamw_scheduled(float* w, float* m, float* v, const float* g,
                                    const float* hyper, float b1, float b2, float eps, float wd, cudaStream_t s) {
     adamw_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, m, v, g, (__nv_bfloat16*)wb, n, 0.0f, b1, b2, eps, wd, 1.0f,
                                                    1.0f, hyper);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bce_bitmask_t(const float* logits, const uint32_t* masks, long long slot_words, int wpr,
+                                 int ncols, int B, int ncells, float scale, void* dlogits, void* dlogits_t,
+                                 long long ldt, float* loss, cudaStream_t s) {
+    dim3 grid((unsigned)(ncells / 64), (unsigned)(B / 64));
+    bce_bitmask_t_kernel<<<grid, 256, 0, s>>>(logits, masks, slot_words, wpr, ncols, ncells, scale,
+                                              (__nv_bfloat16*)dlogits, (__nv_bfloat16*)dlogits_t, ldt, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adamw_t(float* w, float* m, float* v, const float* g, void* wb, void* wbt, long long ldt, int rows,
+                           int cols, const float* hyper, float b1, float b2, float eps, float wd, cudaStream_t s) {
+    dim3 grid((unsigned)(cols / 64), (unsigned)(rows / 64));
+    adamw_t_kernel<<<grid, 256, 0, s>>>(w, m, v, g, (__nv_bfloat16*)wb, (__nv_bfloat16*)wbt, ldt, cols, hyper, b1, b2,
+                                        eps, wd);
     return cudaGetLastError();
 }
 

@@ -6,8 +6,8 @@ per-cell capture logits on the site grid.  It is trained in BF16 with FP32
 master weights on (parameters -> visited-cell mask) pairs that the tracker
 itself chronicles (oneka_track mark-only mode: one bitmask per realization),
 with the project's own kernels: oneka_gemm_bf16 (tensor cores),
-oneka_transpose_bf16, oneka_bce_bitmask, oneka_gelu_backward,
-oneka_colsum_bf16, oneka_adamw.
+oneka_bce_bitmask(_t), oneka_transpose_bf16, oneka_gelu_backward,
+oneka_colsum_bf16, oneka_adamw_scheduled(_t).
 
 Screening: the surrogate's field is the mean of sigmoid(logits) over the
 screened realizations; a held-out fraction (the judges) is always tracked,
@@ -77,6 +77,8 @@ class Layer:
     vb: torch.Tensor
     gw: torch.Tensor       # FP32 gradients
     gb: torch.Tensor
+    wbt: torch.Tensor | None = None   # BF16 W^T [in][out] for the backward pass
+    wbt_valid: bool = False            # wbt equals wb^T (kept by oneka_adamw_scheduled_t)
 
 
 class MLP:
@@ -135,8 +137,18 @@ class MLP:
             a["loss"] = torch.zeros(1, dtype=F32, device=self._X.device)
         loss = a["loss"]
         loss.zero_()
-        C.check(C.load().oneka_bce_bitmask(_p(a["logits"]), _p(masks), slot_words, wpr, ncols, B, ncells,
-                                           1.0 / (B * ncells), _p(a["dlogits"]), _p(loss), C.stream_ptr()))
+        if B % 64 == 0 and ncols % 64 == 0:
+            # the gradient also transposed, [ncells][B]: the last layer's weight-gradient operand
+            if "dlogits_t" not in a:
+                a["dlogits_t"] = torch.empty((ncells, B), dtype=BF16, device=self._X.device)
+            C.check(C.load().oneka_bce_bitmask_t(_p(a["logits"]), _p(masks), slot_words, wpr, ncols, B, ncells,
+                                                 1.0 / (B * ncells), _p(a["dlogits"]), _p(a["dlogits_t"]), B,
+                                                 _p(loss), C.stream_ptr()))
+            self._dlogits_t = True
+        else:
+            C.check(C.load().oneka_bce_bitmask(_p(a["logits"]), _p(masks), slot_words, wpr, ncols, B, ncells,
+                                               1.0 / (B * ncells), _p(a["dlogits"]), _p(loss), C.stream_ptr()))
+            self._dlogits_t = False
         return loss
 
     def _transposed(self, name, rows, cols, device):
@@ -145,13 +157,18 @@ class MLP:
             self._acts[key] = torch.empty((cols, rows), dtype=BF16, device=device)
         return self._acts[key]
 
-    def backward(self):
-        """Gradients of every layer.  The two GEMMs per layer contract over the
-        batch (gW = dZ^T H_in) and over the layer's outputs (dH_in = dZ W);
-        their operands are stored with the contracted index outermost, so they
-        are first transposed (oneka_transpose_bf16, bandwidth-bound) and both
-        GEMMs then run K-major on the tensor cores; dH_in, whose K is the
-        65,536 outputs of the last layer, is split over K."""
+    def backward(self, hyper=None, betas=(0.9, 0.999), eps=1e-8, weight_decay=1e-4):
+        """Gradients of every layer, and with `hyper` (device [lr, 1 - beta1^t,
+        1 - beta2^t]) the AdamW step too.
+
+        The two GEMMs per layer contract over the batch (gW = dZ^T H_in) and
+        over the layer's outputs (dH_in = dZ W); their operands are stored with
+        the contracted index outermost, so they run K-major on the tensor
+        cores from transposed copies: dZ^T of the last layer comes from the
+        loss kernel, W^T from the previous AdamW step (oneka_adamw_scheduled_t
+        keeps it), the rest from oneka_transpose_bf16.  A GEMM with fewer
+        output tiles than SMs is split over K.  A layer's dH_in is computed
+        before its weights are stepped."""
         X = self._X
         B = X.shape[0]
         dev = X.device
@@ -164,30 +181,72 @@ class MLP:
             dout, din = L.w.shape
             hin = X if i == 0 else a["H"][i - 1]
             # gW = dZ^T H_in : [dout][din] = (dZ^T [dout][B]) (H_in^T [din][B])^T
-            dzt = self._transposed(("dz", i), B, dout, dev)
+            if i == n - 1 and getattr(self, "_dlogits_t", False):
+                dzt = a["dlogits_t"]
+            else:
+                dzt = self._transposed(("dz", i), B, dout, dev)
+                C.check(Lb.oneka_transpose_bf16(_p(dcur), B, dout, dcur.shape[-1], _p(dzt), B, C.stream_ptr()))
             hint = self._transposed(("h", i), B, din, dev)
-            C.check(Lb.oneka_transpose_bf16(_p(dcur), B, dout, dcur.shape[-1], _p(dzt), B, C.stream_ptr()))
             C.check(Lb.oneka_transpose_bf16(_p(hin), B, din, hin.shape[-1], _p(hint), B, C.stream_ptr()))
-            gemm(dzt, True, hint, True, L.gw, dout, din, B)
+            tiles_w = -(-dout // 128) * -(-din // 256)
+            splitk = max(1, min(B // 64, round(2 * SM_COUNT / tiles_w))) if B % 64 == 0 else 1
+            if splitk > 1:
+                L.gw.zero_()
+            gemm(dzt, True, hint, True, L.gw, dout, din, B, splitk=splitk)
             C.check(Lb.oneka_colsum_bf16(_p(dcur), B, dout, _p(L.gb), C.stream_ptr()))
-            if i == 0:
+            dz = None
+            if i > 0:
+                # dH_in = dZ W : [B][din] = (dZ [B][dout]) (W^T [din][dout])^T, split over K = dout
+                wt = self._weight_t(L)
+                dh = a["dh"][i - 1]
+                dh.zero_()
+                tiles = -(-B // 128) * -(-din // 256)
+                splitk = max(1, min(dout // 64, round(2 * SM_COUNT / tiles)))
+                gemm(dcur, True, wt, True, dh, B, din, dout, splitk=splitk)
+                dz = a["dz"][i - 1]
+                C.check(Lb.oneka_gelu_backward(_p(dh), _p(a["Z"][i - 1]), _p(dz), dh.numel(), C.stream_ptr()))
+            if hyper is not None:
+                self._step_layer(L, hyper, betas, eps, weight_decay)
+            if dz is None:
                 break
-            # dH_in = dZ W : [B][din] = (dZ [B][dout]) (W^T [din][dout])^T, split over K = dout
-            wt = self._transposed(("w", i), dout, din, dev)
-            C.check(Lb.oneka_transpose_bf16(_p(L.wb), dout, din, din, _p(wt), dout, C.stream_ptr()))
-            dh = a["dh"][i - 1]
-            dh.zero_()
-            tiles = -(-B // 128) * -(-din // 256)
-            splitk = max(1, min(dout // 64, round(2 * SM_COUNT / tiles)))
-            gemm(dcur, True, wt, True, dh, B, din, dout, splitk=splitk)
-            dz = a["dz"][i - 1]
-            C.check(Lb.oneka_gelu_backward(_p(dh), _p(a["Z"][i - 1]), _p(dz), dh.numel(), C.stream_ptr()))
             dcur = dz
+
+    def _step_layer(self, L, hyper, betas, eps, weight_decay):
+        """AdamW step of one layer's weights and bias (schedule in `hyper`)."""
+        Lb = C.load()
+        dout, din = L.w.shape
+        if dout % 64 == 0 and din % 64 == 0:       # the step keeps W^T current
+            C.check(Lb.oneka_adamw_scheduled_t(_p(L.w), _p(L.mw), _p(L.vw), _p(L.gw), _p(L.wb), _p(self._wt_buffer(L)),
+                                               dout, dout, din, _p(hyper), betas[0], betas[1], eps, weight_decay,
+                                               C.stream_ptr()))
+            L.wbt_valid = True
+        else:
+            C.check(Lb.oneka_adamw_scheduled(_p(L.w), _p(L.mw), _p(L.vw), _p(L.gw), _p(L.wb), L.w.numel(), _p(hyper),
+                                             betas[0], betas[1], eps, weight_decay, C.stream_ptr()))
+            L.wbt_valid = False
+        C.check(Lb.oneka_adamw_scheduled(_p(L.b), _p(L.mb), _p(L.vb), _p(L.gb), None, L.b.numel(), _p(hyper),
+                                         betas[0], betas[1], eps, 0.0, C.stream_ptr()))
+
+    def _wt_buffer(self, L):
+        if getattr(L, "wbt", None) is None:
+            L.wbt = torch.empty((L.w.shape[1], L.w.shape[0]), dtype=BF16, device=L.w.device)
+            L.wbt_valid = False
+        return L.wbt
+
+    def _weight_t(self, L):
+        """W^T of layer L in BF16 [din][dout], transposed now unless an
+        oneka_adamw_scheduled_t step has kept it current."""
+        wt = self._wt_buffer(L)
+        if not getattr(L, "wbt_valid", False):
+            dout, din = L.w.shape
+            C.check(C.load().oneka_transpose_bf16(_p(L.wb), dout, din, din, _p(wt), dout, C.stream_ptr()))
+        return wt
 
     def adamw(self, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, weight_decay=1e-4):
         self.step_count += 1
         Lb = C.load()
         for L in self.layers:
+            L.wbt_valid = False
             C.check(Lb.oneka_adamw(_p(L.w), _p(L.mw), _p(L.vw), _p(L.gw), _p(L.wb), L.w.numel(), lr, betas[0],
                                    betas[1], eps, weight_decay, self.step_count, C.stream_ptr()))
             C.check(Lb.oneka_adamw(_p(L.b), _p(L.mb), _p(L.vb), _p(L.gb), None, L.b.numel(), lr, betas[0],
@@ -198,6 +257,7 @@ class MLP:
         tensor hyper = [lr, 1 - beta1^t, 1 - beta2^t] (a captured step)."""
         Lb = C.load()
         for L in self.layers:
+            L.wbt_valid = False
             C.check(Lb.oneka_adamw_scheduled(_p(L.w), _p(L.mw), _p(L.vw), _p(L.gw), _p(L.wb), L.w.numel(),
                                              _p(hyper), betas[0], betas[1], eps, weight_decay, C.stream_ptr()))
             C.check(Lb.oneka_adamw_scheduled(_p(L.b), _p(L.mb), _p(L.vb), _p(L.gb), None, L.b.numel(), _p(hyper),
@@ -320,8 +380,7 @@ def train(model: MLP, X: torch.Tensor, masks: torch.Tensor, slot_words: int, wpr
     def body():
         model.forward(xs)
         model.loss_and_grad(ms, slot_words, wpr, ncols)
-        model.backward()
-        model.adamw_scheduled(hyper, betas, eps, weight_decay)
+        model.backward(hyper, betas, eps, weight_decay)     # gradients and the AdamW step
 
     g = None
     losses = []

@@ -98,6 +98,54 @@ def test_mlp_gradients_match_cpu_oracle():
         assert np.linalg.norm(gb - db[i]) <= 0.03 * np.linalg.norm(db[i]) + 1e-12, i
 
 
+def test_transposing_bce_and_adamw_match_plain_kernels():
+    """oneka_bce_bitmask_t and oneka_adamw_scheduled_t: the plain kernels'
+    results, plus exact transposed BF16 copies."""
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(8)
+    B, nr, nc = 128, 8, 128
+    ncells, wpr = nr * nc, nc // 32
+    slot = nr * wpr
+    logits = (torch.randn((B, ncells), generator=g) * 3).to(dev)
+    masks = torch.randint(-2**31, 2**31 - 1, (B, slot), dtype=torch.int64, generator=g).to(torch.int32).to(dev)
+    Lb = C.load()
+    d1 = torch.empty((B, ncells), dtype=torch.bfloat16, device=dev)
+    d2 = torch.empty_like(d1)
+    dt = torch.empty((ncells, B), dtype=torch.bfloat16, device=dev)
+    l1 = torch.zeros(1, device=dev)
+    l2 = torch.zeros(1, device=dev)
+    C.check(Lb.oneka_bce_bitmask(C.ptr(logits), C.ptr(masks), slot, wpr, nc, B, ncells, 1.0 / (B * ncells), C.ptr(d1),
+                                 C.ptr(l1), C.stream_ptr()))
+    C.check(Lb.oneka_bce_bitmask_t(C.ptr(logits), C.ptr(masks), slot, wpr, nc, B, ncells, 1.0 / (B * ncells),
+                                   C.ptr(d2), C.ptr(dt), B, C.ptr(l2), C.stream_ptr()))
+    torch.cuda.synchronize()
+    assert torch.equal(d1, d2) and torch.equal(dt, d2.T)
+    assert abs(float(l1) - float(l2)) <= 1e-5 * abs(float(l1))
+    rows, cols = 192, 256
+    w0 = (torch.randn((rows, cols), generator=g) * 0.05).to(dev)
+    m0 = (torch.randn((rows, cols), generator=g) * 0.01).to(dev)
+    v0 = (torch.rand((rows, cols), generator=g) * 0.01).to(dev)
+    gr = torch.randn((rows, cols), generator=g).to(dev)
+    hyper = torch.tensor([1e-3, 1 - 0.9 ** 3, 1 - 0.999 ** 3], dtype=torch.float32, device=dev)
+    out = {}
+    for t in (False, True):
+        w, m, v = w0.clone(), m0.clone(), v0.clone()
+        wb = torch.empty((rows, cols), dtype=torch.bfloat16, device=dev)
+        wbt = torch.empty((cols, rows), dtype=torch.bfloat16, device=dev)
+        if t:
+            C.check(Lb.oneka_adamw_scheduled_t(C.ptr(w), C.ptr(m), C.ptr(v), C.ptr(gr), C.ptr(wb), C.ptr(wbt), rows,
+                                               rows, cols, C.ptr(hyper), 0.9, 0.999, 1e-8, 1e-4, C.stream_ptr()))
+        else:
+            C.check(Lb.oneka_adamw_scheduled(C.ptr(w), C.ptr(m), C.ptr(v), C.ptr(gr), C.ptr(wb), rows * cols,
+                                             C.ptr(hyper), 0.9, 0.999, 1e-8, 1e-4, C.stream_ptr()))
+        torch.cuda.synchronize()
+        out[t] = (w, m, v, wb, wbt)
+    for a, b in zip(out[False][:3], out[True][:3]):     # the same update; multiply-adds may contract differently
+        assert torch.allclose(a, b, rtol=1e-5, atol=1e-7), float((a - b).abs().max())
+    assert torch.equal(out[True][4], out[True][3].T)
+    assert float((out[True][3].float() - out[False][3].float()).abs().max()) <= 2 ** -8 * 0.3
+
+
 def test_graph_captured_training_matches_eager():
     """SG.train with the training step captured as a CUDA graph (and its
     schedule read from the device by oneka_adamw_scheduled) follows the
