@@ -298,13 +298,14 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     const int cl = max(left, -coff), cr = min(right, gncols - coff);
     if (rb >= re || cl >= cr) return;
     const float xlo = i2f_small(cl) - 1.0f, xhi = i2f_small(cr);
-    // The row loop, instantiated twice: for a node box that lies wholly in
-    // the shared-memory window (almost every segment near the target) the
-    // marks go there without per-row or per-word window tests.
-    auto rows = [&](auto in_win) {
+    // The row loop, instantiated four times.  IN_WIN: the node box lies wholly
+    // in the shared-memory window (almost every segment near the target), so
+    // the marks go there without per-row or per-word window tests.  GENERAL:
+    // the segment is parallel to neither axis (BAX, BAY != 0), so the band's
+    // limits need no per-row case analysis.
+    auto rows = [&](auto in_win, auto general) {
         float t = i2f_small(rb) * ryy - aY;             // row offset from a (units of dx)
         for (int i = rb; i < re; ++i, t += ryy) {
-            const int gi = i + roff;
             float LO = INFINITY, HI = -INFINITY;
             const float ha = U2 - t * t;
             if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
@@ -312,22 +313,27 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
             const float hb = U2 - tb * tb;
             if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bX - h); HI = fmaxf(HI, bX + h); }
             float slo, shi;
-            if (bay_nz) {
-                const float kt = k * t;
-                slo = kt - ae;
-                shi = kt + ae;
+            if (decltype(general)::value) {
+                slo = fmaxf(k * t - ae, flo - m * t);
+                shi = fminf(k * t + ae, fhi - m * t);
             } else {
-                const bool in = fabsf(t) < U;
-                slo = in ? -INFINITY : INFINITY;
-                shi = in ? INFINITY : -INFINITY;
-            }
-            if (bax_nz) {
-                const float mt = -m * t;
-                slo = fmaxf(slo, mt + flo);
-                shi = fminf(shi, mt + fhi);
-            } else {
-                const float yc = BAY * t;
-                if (!(yc >= 0.0f && yc <= L2)) slo = INFINITY;
+                if (bay_nz) {
+                    const float kt = k * t;
+                    slo = kt - ae;
+                    shi = kt + ae;
+                } else {
+                    const bool in = fabsf(t) < U;
+                    slo = in ? -INFINITY : INFINITY;
+                    shi = in ? INFINITY : -INFINITY;
+                }
+                if (bax_nz) {
+                    const float mt = -m * t;
+                    slo = fmaxf(slo, mt + flo);
+                    shi = fminf(shi, mt + fhi);
+                } else {
+                    const float yc = BAY * t;
+                    if (!(yc >= 0.0f && yc <= L2)) slo = INFINITY;
+                }
             }
             if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
             if (!(LO < HI)) continue;
@@ -336,17 +342,21 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
             const int jlo = floor_bounded(fmaxf(LO, xlo)) + 1;
             const int jhi = ceil_bounded(fminf(HI, xhi)) - 1;
             if (jlo > jhi) continue;
-            or_span<decltype(in_win)::value>(ch, gi, jlo + coff, jhi + coff, natom);
-            rlo = gi < rlo ? gi : rlo;
-            rhi = gi > rhi ? gi : rhi;
+            or_span<decltype(in_win)::value>(ch, i + roff, jlo + coff, jhi + coff, natom);
         }
     };
+    // the slot header bounds the rows that may hold marks: the segment's row range
+    rlo = min(rlo, rb + roff);
+    rhi = max(rhi, re - 1 + roff);
     const bool in_win = ch.win && rb + roff >= ch.r0 && re + roff <= ch.r0 + ch.nr &&
                         ((cl + coff) >> 5) >= ch.w0 && ((cr - 1 + coff) >> 5) < ch.w0 + ch.nw;
-    if (in_win)
-        rows(std::true_type{});
-    else
-        rows(std::false_type{});
+    if (bay_nz && bax_nz) {
+        if (in_win) rows(std::true_type{}, std::true_type{});
+        else rows(std::false_type{}, std::true_type{});
+    } else {
+        if (in_win) rows(std::true_type{}, std::false_type{});
+        else rows(std::false_type{}, std::false_type{});
+    }
 }
 
 
