@@ -182,15 +182,6 @@ __device__ __forceinline__ int floor_small(float x) {
     return (__float_as_int(b) - kMagicBits) - (r > x ? 1 : 0);
 }
 
-// floor / ceil of a finite x already known to lie within +-2^22 (no clamp).
-__device__ __forceinline__ int floor_bounded(float x) {
-    const float b = __fadd_rn(x, kMagic);
-    const float r = __fsub_rn(b, kMagic);
-    return (__float_as_int(b) - kMagicBits) - (r > x ? 1 : 0);
-}
-
-__device__ __forceinline__ int ceil_bounded(float x) { return -floor_bounded(-x); }
-
 // clip_range for integer bounds [lo, hi) of a range of n nodes.
 __device__ __forceinline__ bool clip_int(int lo, int hi, int n, int& ilo, int& ihi) {
     ilo = lo < 0 ? 0 : lo;
@@ -210,11 +201,14 @@ __device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int gh
         const int wl = ghi >> 5;
         natom += wl - w + 1;
         uint32_t m = 0xffffffffu << (glo & 31);
-        for (; w <= wl; ++w) {
-            if (w == wl) m &= 0xffffffffu >> (31 - (ghi & 31));
-            atomicOr(ch.win + (base + w), m);
-            m = 0xffffffffu;
+        const uint32_t mlast = 0xffffffffu >> (31 - (ghi & 31));
+        if (w == wl) {                       // most spans lie in one word
+            atomicOr(ch.win + (base + w), m & mlast);
+            return;
         }
+        atomicOr(ch.win + (base + w), m);
+        for (++w; w < wl; ++w) atomicOr(ch.win + (base + w), 0xffffffffu);
+        atomicOr(ch.win + (base + wl), mlast);
         return;
     }
     const int ri = gi - ch.r0;
@@ -338,9 +332,12 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
             if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
             if (!(LO < HI)) continue;
             // nodes strictly inside (LO, HI), within the columns [cl, cr); LO < HI
-            // here, so both clamped ends are finite and within [cl - 1, cr]
-            const int jlo = floor_bounded(fmaxf(LO, xlo)) + 1;
-            const int jhi = ceil_bounded(fminf(HI, xhi)) - 1;
+            // here, so both clamped ends are finite and within [cl - 1, cr].  The
+            // integer nearest x - 1/2 is floor(x) except for an integer x, where the
+            // tie may round down: a node exactly at umbra from the segment, inside
+            // the FP32 build's boundary tolerance, may then be marked.
+            const int jlo = __float_as_int(__fadd_rn(fmaxf(LO, xlo) - 0.5f, kMagic)) - (kMagicBits - 1);
+            const int jhi = __float_as_int(__fadd_rn(fminf(HI, xhi) + 0.5f, kMagic)) - (kMagicBits + 1);
             if (jlo > jhi) continue;
             or_span<decltype(in_win)::value>(ch, i + roff, jlo + coff, jhi + coff, natom);
         }
