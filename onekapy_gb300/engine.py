@@ -163,15 +163,26 @@ def replay_expand(xo, yo, dx, dy, bboxes, grid0=None):
             float(sy1[ky1[-1]])), frames
 
 
+_rings: dict = {}
+
+
 def release_ring(xtarget, ytarget, rtarget, npaths) -> np.ndarray:
     """Release points of compute_capturezone (oneka/capturezone.py:110-115),
-    evaluated element by element with NumPy exactly as the reference does."""
-    STEPAWAY = 1.0
-    out = np.empty((npaths, 2), dtype=np.float64)
-    for i, theta in enumerate(np.linspace(0, 2 * np.pi, npaths + 1)[0:-1]):
-        out[i, 0] = (rtarget + STEPAWAY) * np.cos(theta) + xtarget
-        out[i, 1] = (rtarget + STEPAWAY) * np.sin(theta) + ytarget
-    return out
+    evaluated element by element with NumPy exactly as the reference does
+    (NumPy's scalar cos/sin; its vectorized ones may round differently).
+    Rings are cached per (target, radius, npaths); a copy is returned."""
+    key = (float(xtarget), float(ytarget), float(rtarget), int(npaths))
+    ring = _rings.get(key)
+    if ring is None:
+        STEPAWAY = 1.0
+        ring = np.empty((npaths, 2), dtype=np.float64)
+        for i, theta in enumerate(np.linspace(0, 2 * np.pi, npaths + 1)[0:-1]):
+            ring[i, 0] = (rtarget + STEPAWAY) * np.cos(theta) + xtarget
+            ring[i, 1] = (rtarget + STEPAWAY) * np.sin(theta) + ytarget
+        if len(_rings) > 64:
+            _rings.clear()
+        _rings[key] = ring
+    return ring.copy()
 
 
 # ---------------------------------------------------------------------------

@@ -92,6 +92,7 @@ class ProbabilityField:
         self._pdev = torch.zeros((self.nrows, self.ncols), dtype=torch.float64, device=dev)
         self._phost = None
         self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=dev)
+        self._mask_clean = True     # no bit set since the last register / reset
 
     @property
     def pgrid(self) -> np.ndarray | None:
@@ -100,7 +101,10 @@ class ProbabilityField:
         if self._pdev is None:
             return self._phost
         if self._phost is None:
-            self._phost = self._pdev.cpu().numpy()
+            # through page-locked memory (torch caches those blocks): a direct DMA copy
+            host = torch.empty(self._pdev.shape, dtype=torch.float64, pin_memory=True)
+            host.copy_(self._pdev)
+            self._phost = host.numpy()
         return self._phost
 
     @pgrid.setter
@@ -133,10 +137,13 @@ class ProbabilityField:
         v = torch.as_tensor(np.asarray(value) if not isinstance(value, torch.Tensor) else value,
                             device=self._mask.device).to(torch.bool)
         self._mask = _pack(v, (self.ncols + 31) // 32, self._mask_words())
+        self._mask_clean = False
 
     @property
     def mask(self) -> torch.Tensor:
-        """The registration bitmask (device int32 words, row-major)."""
+        """The registration bitmask (device int32 words, row-major); a caller
+        may mark nodes in it (oneka_track's mark-only mode)."""
+        self._mask_clean = False
         return self._mask
 
     def __repr__(self):
@@ -188,10 +195,16 @@ class ProbabilityField:
             self._regrid(nrows, ncols, rshift, cshift)
 
     def _regrid(self, nrows, ncols, rshift, cshift):
-        old_r = self.rgrid_device
         dev = self._pdev.device
         pgrid = torch.zeros((nrows, ncols), dtype=torch.float64, device=dev)
         pgrid[rshift:rshift + self.nrows, cshift:cshift + self.ncols] = self._pdev
+        if getattr(self, "_mask_clean", False):     # nothing to carry over: a fresh mask
+            self._pdev = pgrid
+            self._phost = None
+            self.nrows, self.ncols = nrows, ncols
+            self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=dev)
+            return
+        old_r = self.rgrid_device
         rgrid = torch.zeros((nrows, ncols), dtype=torch.bool, device=dev)
         rgrid[rshift:rshift + self.nrows, cshift:cshift + self.ncols] = old_r
         self._pdev = pgrid
@@ -216,6 +229,7 @@ class ProbabilityField:
         dev = self._mask.device
         t = torch.as_tensor(np.ascontiguousarray(xy, dtype=np.float64), device=dev)
         g = self._grid().c()
+        self._mask_clean = False
         C.check(C.load().oneka_rasterize(ctypes.byref(g), ctypes.byref(frame) if frame else None,
                                          C.ptr(t), t.shape[0], float(umbra), C.ptr(self._mask),
                                          C.stream_ptr()))
@@ -227,10 +241,12 @@ class ProbabilityField:
         C.check(C.load().oneka_register_weighted(ctypes.byref(g), C.ptr(self._mask), float(weight),
                                                  C.ptr(self._pdev), C.stream_ptr()))
         self._phost = None
+        self._mask_clean = True
 
     def reset(self):
         """Clear rgrid (probabilityfield.py:362-376)."""
         self._mask.zero_()
+        self._mask_clean = True
 
     @staticmethod
     def distancesquared(ax, ay, bx, by, cx, cy):
@@ -267,6 +283,7 @@ class ProbabilityField:
         if torch.cuda.is_available():
             self.pgrid = pgrid
             self._mask = torch.zeros(self._mask_words(), dtype=torch.int32, device=C.device())
+            self._mask_clean = True
             self.rgrid = rgrid
         else:           # inspection without a GPU: host arrays only
             self._phost = np.asarray(pgrid, dtype=np.float64)
