@@ -31,6 +31,9 @@ __device__ __forceinline__ void register_slot(uint32_t* __restrict__ slot, long 
         slot[w] = 0u;
         const int row = (int)(w / wpr);
         const int col0 = (int)(w % wpr) * 32;
+        // bits past the last column are never set by the trackers; dropping
+        // them keeps a stray one from counting into the next row
+        if (ncols - col0 < 32) v &= (1u << (ncols - col0)) - 1u;
         int32_t* crow = counts + (long long)row * ncols + col0;
         while (v) {
             const int b = __ffs(v) - 1;

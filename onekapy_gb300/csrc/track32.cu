@@ -75,11 +75,15 @@ struct Kahan {
 };
 
 // Kahan summation of (x, y) pairs; the compensation is kept negated, so the
-// total is s + cn and every step is one packed instruction.
+// total is s + cn and every step is one packed instruction.  Terms are added
+// in groups: a group's products are chained by FMA onto the compensation
+// (one rounding per term, as a per-term Kahan step has) and the group enters
+// the running sum with one compensated addition, so the rounding of the
+// large running sum is still recovered while the compensation costs three
+// instructions per group instead of per term.
 struct Kahan2 {
     float2 s, cn;
-    __device__ __forceinline__ void add_prod(float2 a, float2 b) {   // += a * b
-        const float2 y = fma2(a, b, cn);
+    __device__ __forceinline__ void add(float2 y) {   // += y, where y already carries cn
         const float2 t = add2(s, y);
         cn = rsub2(rsub2(s, t), y);     // y - (t - s)
         s = t;
@@ -103,16 +107,15 @@ __device__ __forceinline__ bool feval32(const Model32& m, float2 ph, float2 pl, 
     Kahan pot{0.0f, 0.0f};
     if (!CONFINED)
         pot.s = m.c0 * dxo * dxo + m.c1 * dyo * dyo + m.c2 * dxo * dyo + m.c3 * dxo + m.c4 * dyo + m.c5;
-#pragma unroll 4
-    for (int i = 0; i < m.nw; ++i) {
+    // well i's discharge term onto y, its potential term into pot; wq = its
+    // constants (-q/(2 pi), q ln(2)/(4 pi))
+    auto well = [&](int i, float2 wq, float2 y) {
         const float4 w = m.wp[i];
-        const float2 wq = m.wq[i];
         // recentred difference: (x_hi - xw_hi) + (x_lo - xw_lo), both coordinates at once
         const float2 d = add2(add2(ph, make_float2(w.x, w.y)), add2(pl, make_float2(w.z, w.w)));
         const float r2 = d.x * d.x + d.y * d.y;
-        q.add_prod(splat(__fdividef(wq.x, r2)), d);
-        // q/(4 pi) ln r^2 (ln 2 folded into wq.y).  The discharge sums above
-        // carry the trace's accuracy and are compensated; the potential only
+        // q/(4 pi) ln r^2 (ln 2 folded into wq.y).  The discharge sums carry
+        // the trace's accuracy and are compensated; the potential only
         // selects the head branch and scales the velocity, and compensating
         // it changed no measured drift, so it is compensated only where the
         // FP64 head inversion reads the unrounded pair.
@@ -122,6 +125,33 @@ __device__ __forceinline__ bool feval32(const Model32& m, float2 ph, float2 pl, 
             else
                 pot.s += wq.y * __log2f(r2);
         }
+        return fma2(splat(__fdividef(wq.x, r2)), d, y);
+    };
+    // the constants of wells 2j and 2j + 1 in one 16-byte load (the array
+    // is padded to whole float4s)
+    const float4* wq4 = reinterpret_cast<const float4*>(m.wq);
+    constexpr int G = 4;       // wells per compensated group
+    int i = 0;
+#pragma unroll 1
+    for (; i + G <= m.nw; i += G) {
+        const float4 qa = wq4[i >> 1], qb = wq4[(i >> 1) + 1];
+        float2 y = q.cn;
+        y = well(i, make_float2(qa.x, qa.y), y);
+        y = well(i + 1, make_float2(qa.z, qa.w), y);
+        y = well(i + 2, make_float2(qb.x, qb.y), y);
+        y = well(i + 3, make_float2(qb.z, qb.w), y);
+        q.add(y);
+    }
+    if (i < m.nw) {            // the last, partial group
+        float2 y = q.cn;
+#pragma unroll 1
+        for (; i + 1 < m.nw; i += 2) {
+            const float4 qa = wq4[i >> 1];
+            y = well(i, make_float2(qa.x, qa.y), y);
+            y = well(i + 1, make_float2(qa.z, qa.w), y);
+        }
+        if (i < m.nw) y = well(i, m.wq[i], y);
+        q.add(y);
     }
     const float2 qt = add2(q.s, q.cn);
     if (CONFINED) {
@@ -189,36 +219,36 @@ __device__ __forceinline__ bool clip_int(int lo, int hi, int n, int& ilo, int& i
     return ilo < ihi;
 }
 
-// OR the nodes gj in [glo, ghi] of grid row gi into the chronicle.  IN_WIN:
-// the caller has established that the whole span lies in the shared-memory
-// window, so no test is made.  Otherwise the row's window test is made once
-// and each word's once.
-template <bool IN_WIN>
-__device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int ghi, unsigned& natom) {
-    if (IN_WIN) {
-        const int base = (gi - ch.r0) * ch.nw - ch.w0;
-        int w = glo >> 5;
-        const int wl = ghi >> 5;
-        natom += wl - w + 1;
-        uint32_t m = 0xffffffffu << (glo & 31);
-        const uint32_t mlast = 0xffffffffu >> (31 - (ghi & 31));
-        if (w == wl) {                       // most spans lie in one word
-            atomicOr(ch.win + (base + w), m & mlast);
-            return;
-        }
-        atomicOr(ch.win + (base + w), m);
-        for (++w; w < wl; ++w) atomicOr(ch.win + (base + w), 0xffffffffu);
-        atomicOr(ch.win + (base + wl), mlast);
+// OR the nodes gj in [glo, ghi] of one grid row into the chronicle.
+// or_win: the caller has established that the whole span lies in the
+// shared-memory window, whose word (row, 0) is at ch.win + base.  or_span:
+// otherwise; the row's window test is made once and each word's once.
+// Masks: bits lo.. of a word are 0 - (1 << lo), bits ..hi are (2 << hi) - 1
+// (2 << 31 wraps to 0), bits lo..hi of one word (2 << hi) - (1 << lo).
+__device__ __forceinline__ void or_win(const Chron& ch, int base, int glo, int ghi, unsigned& natom) {
+    int w = glo >> 5;
+    const int wl = ghi >> 5;
+    natom += wl - w + 1;
+    const uint32_t lo_bit = 1u << (glo & 31);
+    const uint32_t hi_end = 2u << (ghi & 31);
+    if (w == wl) {                       // most spans lie in one word
+        atomicOr(ch.win + (base + w), hi_end - lo_bit);
         return;
     }
+    atomicOr(ch.win + (base + w), 0u - lo_bit);
+    for (++w; w < wl; ++w) atomicOr(ch.win + (base + w), 0xffffffffu);
+    atomicOr(ch.win + (base + wl), hi_end - 1u);
+}
+
+__device__ __forceinline__ void or_span(const Chron& ch, int gi, int glo, int ghi, unsigned& natom) {
     const int ri = gi - ch.r0;
     const bool row_in = ch.win && (unsigned)ri < (unsigned)ch.nr;
     int w = glo >> 5;
     const int wl = ghi >> 5;
     natom += wl - w + 1;
-    uint32_t m = 0xffffffffu << (glo & 31);
+    uint32_t m = 0u - (1u << (glo & 31));
     for (; w <= wl; ++w) {
-        if (w == wl) m &= 0xffffffffu >> (31 - (ghi & 31));
+        if (w == wl) m &= (2u << (ghi & 31)) - 1u;
         const int wi = w - ch.w0;
         if (row_in && (unsigned)wi < (unsigned)ch.nw)
             atomicOr(ch.win + ri * ch.nw + wi, m);
@@ -238,11 +268,22 @@ struct Raster32 {
 
 // Chronicle one segment in FP32: for every grid row the nodes within umbra
 // of the segment form one open interval (LO, HI), the row's intersection
-// with the capsule (the two end disks and the band between them); its nodes
-// floor(LO) + 1 .. ceil(HI) - 1 are set as whole bit ranges.  Nodes strictly
+// with the capsule (the band and the end disk at b; see below for the disk
+// at a); its nodes floor(LO) + 1 .. ceil(HI) - 1 are set as whole bit
+// ranges.  Nodes strictly
 // closer than umbra are marked, as in ProbabilityField.insert
 // (probabilityfield.py:296-310); FP32 rounding can move a node lying within
-// ~1e-6 m of the boundary across it.
+// a few ulps of its frame coordinate (about 1e-4 of a cell on a 1,601-node
+// frame) of the boundary across it.
+//
+// A trace's capsules overlap at their joints: segment i starts where the
+// last segment of nonzero length before it ended, whose capsule holds the
+// disk about that point, so a segment does not mark the disk about its
+// start a.  The one disk no segment marks, about the release point, is
+// marked by disk32 once per trace (after the block's traces end), for every
+// trace with a segment that reached the row loop; a trace whose segments
+// were all clipped away has no node of that disk in its frame.  The union of
+// the marks is the reference's (in exact arithmetic).
 //
 // Geometry is in units of dx with x measured from the frame's first column,
 // so LO and HI are node indices; every per-row quantity is one multiply-add
@@ -291,7 +332,23 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     const int rb = max(bottom, -roff), re = min(top, gnrows - roff);
     const int cl = max(left, -coff), cr = min(right, gncols - coff);
     if (rb >= re || cl >= cr) return;
-    const float xlo = i2f_small(cl) - 1.0f, xhi = i2f_small(cr);
+    // Node spans: the nodes strictly inside (LO, HI) are the integers from
+    // nearest(LO - 1/2) + 1 to nearest(HI + 1/2) - 1 (floor(LO) + 1 and
+    // ceil(HI) - 1, except at an integer LO or HI, where the tie may round
+    // toward the interval: a node exactly at umbra from the segment, inside
+    // the FP32 build's boundary tolerance, may then be marked).  The halves
+    // are folded into the interval's ends (aXm, aXp, ... below) and the
+    // column offset into the constants that take the integer out of the
+    // rounded sum; these roundings move the boundary by an ulp of the
+    // interval's ends, within the same tolerance.  The clamp to the columns
+    // [cl, cr) is a quarter node inside cl - 1 and cr, never a tie, so it
+    // gives exactly cl and cr - 1 (a clamp at cl - 1 would be the tie
+    // cl - 3/2, which rounds to even and can reach column cl - 1).  An empty
+    // row needs no test of its own: LO = +inf, HI = -inf give glo > ghi, and
+    // so does LO >= HI up to the tie above.
+    const float xlo = i2f_small(cl) - 1.25f, xhi = i2f_small(cr) + 0.25f;
+    const float aXm = aX - 0.5f, aXp = aX + 0.5f, bXm = bX - 0.5f, bXp = bX + 0.5f;
+    const int klo = (kMagicBits - 1) - coff, khi = (kMagicBits + 1) - coff;
     // The row loop, instantiated four times.  IN_WIN: the node box lies wholly
     // in the shared-memory window (almost every segment near the target), so
     // the marks go there without per-row or per-word window tests.  GENERAL:
@@ -299,13 +356,12 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     // limits need no per-row case analysis.
     auto rows = [&](auto in_win, auto general) {
         float t = i2f_small(rb) * ryy - aY;             // row offset from a (units of dx)
+        int base = decltype(in_win)::value ? (rb + roff - ch.r0) * ch.nw - ch.w0 : 0;
         for (int i = rb; i < re; ++i, t += ryy) {
-            float LO = INFINITY, HI = -INFINITY;
-            const float ha = U2 - t * t;
-            if (ha > 0.0f) { const float h = sqrtf(ha); LO = aX - h; HI = aX + h; }
+            float LO = INFINITY, HI = -INFINITY;        // the interval's ends, less and plus 1/2
             const float tb = t - BAY;
             const float hb = U2 - tb * tb;
-            if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bX - h); HI = fmaxf(HI, bX + h); }
+            if (hb > 0.0f) { const float h = sqrtf(hb); LO = fminf(LO, bXm - h); HI = fmaxf(HI, bXp + h); }
             float slo, shi;
             if (decltype(general)::value) {
                 slo = fmaxf(k * t - ae, flo - m * t);
@@ -329,17 +385,14 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
                     if (!(yc >= 0.0f && yc <= L2)) slo = INFINITY;
                 }
             }
-            if (slo < shi) { LO = fminf(LO, aX + slo); HI = fmaxf(HI, aX + shi); }
-            if (!(LO < HI)) continue;
-            // nodes strictly inside (LO, HI), within the columns [cl, cr); LO < HI
-            // here, so both clamped ends are finite and within [cl - 1, cr].  The
-            // integer nearest x - 1/2 is floor(x) except for an integer x, where the
-            // tie may round down: a node exactly at umbra from the segment, inside
-            // the FP32 build's boundary tolerance, may then be marked.
-            const int jlo = __float_as_int(__fadd_rn(fmaxf(LO, xlo) - 0.5f, kMagic)) - (kMagicBits - 1);
-            const int jhi = __float_as_int(__fadd_rn(fminf(HI, xhi) + 0.5f, kMagic)) - (kMagicBits + 1);
-            if (jlo > jhi) continue;
-            or_span<decltype(in_win)::value>(ch, i + roff, jlo + coff, jhi + coff, natom);
+            if (slo < shi) { LO = fminf(LO, aXm + slo); HI = fmaxf(HI, aXp + shi); }
+            const int glo = __float_as_int(__fadd_rn(fmaxf(LO, xlo), kMagic)) - klo;
+            const int ghi = __float_as_int(__fadd_rn(fminf(HI, xhi), kMagic)) - khi;
+            if (glo <= ghi) {
+                if (decltype(in_win)::value) or_win(ch, base, glo, ghi, natom);
+                else or_span(ch, i + roff, glo, ghi, natom);
+            }
+            if (decltype(in_win)::value) base += ch.nw;
         }
     };
     // the slot header bounds the rows that may hold marks: the segment's row range
@@ -356,6 +409,41 @@ __device__ __forceinline__ void insert32(const Chron& ch, int gnrows, int gncols
     }
 }
 
+
+// Chronicle the nodes strictly within umbra of the point (ax, ay) (the
+// release point's disk; the same row-interval form as insert32), and return
+// the rows it may have marked in [rlo, rhi].
+__device__ __forceinline__ void disk32(const Chron& ch, int gnrows, int gncols, int coff, int roff, int fncols,
+                                       int fnrows, float fx0, float fy0, const Raster32& g, float ax, float ay,
+                                       int& rlo, int& rhi) {
+    const float umbra = g.umbra, inv_dx = g.inv_dx, inv_dy = g.inv_dy, U2 = g.U2, ryy = g.ryy;
+    int left, right, bottom, top;
+    if (!clip_int(floor_small((ax - umbra - fx0) * inv_dx), floor_small((ax + umbra - fx0) * inv_dx) + 1, fncols,
+                  left, right))
+        return;
+    if (!clip_int(floor_small((ay - umbra - fy0) * inv_dy), floor_small((ay + umbra - fy0) * inv_dy) + 1, fnrows,
+                  bottom, top))
+        return;
+    const int rb = max(bottom, -roff), re = min(top, gnrows - roff);
+    const int cl = max(left, -coff), cr = min(right, gncols - coff);
+    if (rb >= re || cl >= cr) return;
+    const float aX = (ax - fx0) * inv_dx, aY = (ay - fy0) * inv_dx;
+    const float xlo = i2f_small(cl) - 1.25f, xhi = i2f_small(cr) + 0.25f;
+    const float aXm = aX - 0.5f, aXp = aX + 0.5f;
+    const int klo = (kMagicBits - 1) - coff, khi = (kMagicBits + 1) - coff;
+    unsigned natom = 0;
+    float t = i2f_small(rb) * ryy - aY;
+    for (int i = rb; i < re; ++i, t += ryy) {
+        const float ha = U2 - t * t;
+        if (!(ha > 0.0f)) continue;
+        const float h = sqrtf(ha);
+        const int glo = __float_as_int(__fadd_rn(fmaxf(aXm - h, xlo), kMagic)) - klo;
+        const int ghi = __float_as_int(__fadd_rn(fminf(aXp + h, xhi), kMagic)) - khi;
+        if (glo <= ghi) or_span(ch, i + roff, glo, ghi, natom);
+    }
+    rlo = rb + roff;
+    rhi = re - 1 + roff;
+}
 
 // Dormand-Prince tableau in FP32 (capturezone.py:202-209), arranged for
 // running sums.  Row s = 0..5 is the stage point of k_{s+2} (row 5 is the
@@ -399,6 +487,10 @@ struct RealConst32 {
 // float4 slots of a block's well arrays: positions [nw] float4, then
 // constants [nw] float2 rounded up to whole float4s.
 __host__ __device__ __forceinline__ int well_float4s(int nw) { return nw + (nw + 1) / 2; }
+
+// Most particles one block traces (a launch splits larger realizations into
+// chunks), so that its release-disk flags take at most 1 KB of shared memory.
+constexpr int kMaxChunk = 8192;
 
 // Per-lane particle state.  Everything the step loop touches is FP32: on
 // GB300 the FP64 pipe runs at ~1/64 of the FP32 rate, so a handful of FP64
@@ -449,11 +541,14 @@ __device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* wp,
     return feval32<MODE>(m, ph, pl, k);
 }
 
-// Write the finished particle's outputs.
+// Write the finished particle's outputs, and flag its release-point disk
+// for marking (relmask: bit p - pbeg) when one of its segments reached the
+// row loop.
 template <int BLOCK>
 __device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Particle32& s, const Cold<BLOCK>& c,
-                                         const Chron& ch) {
+                                         const Chron& ch, uint32_t* relmask, int pbeg) {
     const long long idx = (long long)r * L.npaths + s.p;
+    if (c.i(kRlo) != 0x7fffffff) atomicOr(relmask + ((s.p - pbeg) >> 5), 1u << ((s.p - pbeg) & 31));
     if (L.out.endpoint) {
         L.out.endpoint[2 * idx] = L.xt + ((double)s.ph.x + (double)s.pl.x);
         L.out.endpoint[2 * idx + 1] = L.yt + ((double)s.ph.y + (double)s.pl.y);
@@ -621,9 +716,10 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     Cold<BLOCK> cold;
     cold.base = reinterpret_cast<uint32_t*>(sm32 + well_float4s(L.nwells));
     uint32_t* slot = L.slots ? L.slots + (long long)k * L.slot_words : nullptr;
-    const Chron ch = make_chron(L, slot, cold.base + kColdFields * BLOCK);
     // particles [pbeg, pend) of this block
     const int per = (L.npaths + chunks - 1) / chunks;
+    uint32_t* relmask = cold.base + kColdFields * BLOCK;        // [ceil(per / 32)] release-disk flags
+    const Chron ch = make_chron(L, slot, relmask + (per + 31) / 32);
     const int pbeg = chunk * per;
     const int pend = min(L.npaths, pbeg + per);
     if (threadIdx.x == 0) {
@@ -658,6 +754,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
                             (float)(q * (0.07957747154594767 * 0.69314718055994531)));
     }
     window_clear(ch);
+    for (int i = threadIdx.x; i < (per + 31) / 32; i += BLOCK) relmask[i] = 0u;
     __syncthreads();
     if (rc.skip) {
         if (L.out.status)
@@ -672,7 +769,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     while (s.p < pend && !live) {
         live = start32<MODE, BLOCK>(L, r, rc, wp, wq, s, cold);
         if (!live) {
-            finish32<BLOCK>(L, r, s, cold, ch);
+            finish32<BLOCK>(L, r, s, cold, ch, relmask, pbeg);
             s.p = atomicAdd(&rc.next, 1);
         }
     }
@@ -683,9 +780,26 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
         if (!live) continue;
         live = attempt32<MODE, BLOCK>(L, rc, wp, wq, ch, s, r, cold);
         while (!live && s.p < pend) {
-            finish32<BLOCK>(L, r, s, cold, ch);
+            finish32<BLOCK>(L, r, s, cold, ch, relmask, pbeg);
             s.p = atomicAdd(&rc.next, 1);
             if (s.p < pend) live = start32<MODE, BLOCK>(L, r, rc, wp, wq, s, cold);
+        }
+    }
+    __syncthreads();
+    // The release-point disks of the flagged traces, all lanes together.  (The
+    // test stays outside the loop: folded into the loop condition it made
+    // the compiled kernel issue 1.8 % more instructions.)
+    if (ch.slot) {
+        for (int p = pbeg + threadIdx.x; p < pend; p += BLOCK) {
+            if (!((relmask[(p - pbeg) >> 5] >> ((p - pbeg) & 31)) & 1u)) continue;
+            const double rx = L.release[2 * p] - L.xt, ry = L.release[2 * p + 1] - L.yt;
+            const float2 h = make_float2((float)rx, (float)ry);
+            const float2 a = add2(h, make_float2((float)(rx - (double)h.x), (float)(ry - (double)h.y)));
+            const OnekaFrame f = frame_of(L, r, p);
+            int rlo = 0x7fffffff, rhi = -1;
+            disk32(ch, L.grid.nrows, L.grid.ncols, f.coff, f.roff, f.ncols, f.nrows, (float)(f.xmin - L.xt),
+                   (float)(f.ymin - L.yt), rc.g, a.x, a.y, rlo, rhi);
+            note_rows(ch.slot, L.mask_words, L.grid.nrows, rlo, rhi);
         }
     }
     __syncthreads();
@@ -730,7 +844,8 @@ cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    // split realizations into particle chunks only when they cannot fill the GPU
+    // split realizations into particle chunks only when they cannot fill the
+    // GPU, and so that no block takes more than kMaxChunk particles
     const int target = 2 * sms * MINB;
     int chunks = 1;
     if (L.nr < target) {
@@ -739,8 +854,10 @@ cudaError_t launch_variant(const TrackLaunch& L, cudaStream_t s) {
         if (chunks > maxc) chunks = maxc;
         if (chunks < 1) chunks = 1;
     }
+    chunks = max(chunks, (L.npaths + kMaxChunk - 1) / kMaxChunk);
+    const int per = (L.npaths + chunks - 1) / chunks;
     const size_t smem = sizeof(float4) * (size_t)well_float4s(L.nwells) + 4 * (size_t)kColdFields * BLOCK +
-                        4 * (size_t)L.win_rows * L.win_words;
+                        4 * (size_t)((per + 31) / 32) + 4 * (size_t)L.win_rows * L.win_words;
     auto kern = track32_kernel<MODE, BLOCK, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -773,8 +890,11 @@ cudaError_t launch_batch_variant(const JobTable& T, int rows, size_t smem, cudaS
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    int minp = 1 << 30;
-    for (int j = 0; j < T.njobs; ++j) minp = min(minp, T.job[j].npaths);
+    int minp = 1 << 30, maxp = 0;
+    for (int j = 0; j < T.njobs; ++j) {
+        minp = min(minp, T.job[j].npaths);
+        maxp = max(maxp, T.job[j].npaths);
+    }
     const int target = 2 * sms * MINB;
     int chunks = 1;
     if (rows < target) {
@@ -783,6 +903,8 @@ cudaError_t launch_batch_variant(const JobTable& T, int rows, size_t smem, cudaS
         if (chunks > maxc) chunks = maxc;
         if (chunks < 1) chunks = 1;
     }
+    chunks = max(chunks, (maxp + kMaxChunk - 1) / kMaxChunk);
+    smem += 4 * (size_t)(((maxp + chunks - 1) / chunks + 31) / 32);   // the release-disk flags
     auto kern = track32_batch_kernel<BLOCK, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

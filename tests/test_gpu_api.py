@@ -93,6 +93,56 @@ def test_config1_full_fp64_bit_exact_vs_oracle(oracle_mod):
     assert linf <= 0.01, linf
 
 
+@pytest.mark.parametrize("ncols,window_kb", [(64, 0), (65, 0), (64, -1), (65, -1)])
+def test_fp32_chronicle_at_the_grid_edges(ncols, window_kb):
+    """A 61 x ncols window about the target that every trace leaves on all
+    sides: the FP32 chronicle marks nothing outside the grid (no bit past a
+    row's last column, no word outside its realization's slot), its node sets
+    differ from the FP64 build's only at umbra-boundary ties, and the
+    registered counts are the masks' sums.  window_kb 0 runs the rows through
+    the shared-memory window (it covers this grid), -1 straight to the slot;
+    ncols 64 has no padding bits (a stray mark lands on a neighbouring row's
+    node), 65 has 31 (an odd right clamp)."""
+    spec = S.config2(nreal=48, npaths=512)
+    site = _site(spec)
+    real = E.realize(site, spec.nreal, seed=2025)
+    sp = spec.spacing
+    nrows = 61
+    grid = E.Grid(site.xt - 30.3 * sp, site.yt - 30.6 * sp, sp, sp, nrows, ncols)
+    dev = site.device
+    rel = torch.as_tensor(site.release(spec.npaths), device=dev)
+    words = grid.slot_bytes() // 4
+    wpr = grid.words_per_row
+    masks = {}
+    for prec in (C.FP32, C.FP64):
+        opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                              confined=spec.confined, precision=prec, window_kb=window_kb)
+        buf = torch.zeros((real.n + 2, words), dtype=torch.int32, device=dev)   # a guard slot either side
+        out = E.TrackOutputs(counters=torch.zeros(E.COUNTERS, dtype=torch.int64, device=dev))
+        E.track(site, real, rel, opts, grid, mark_only=buf[1:-1], outputs=out)
+        b = buf.cpu().numpy().view(np.uint32)
+        assert not b[0].any() and not b[-1].any(), "a mark outside the realizations' slots"
+        m = b[1:-1, :nrows * wpr].reshape(real.n, nrows, wpr)
+        assert not b[1:-1, nrows * wpr:words - 4].any(), "a mark in the slot's padding words"
+        if ncols % 32:
+            assert not (m[:, :, -1] >> (ncols % 32)).any(), "a mark past the last column"
+        masks[prec] = m
+        assert int(out.counters[6].item()) > 0          # traces left the grid
+    bits = lambda a: np.unpackbits(a.view(np.uint8), bitorder="little").reshape(real.n, nrows, -1)[:, :, :ncols]
+    v32, v64 = bits(masks[C.FP32]), bits(masks[C.FP64])
+    assert v64.sum() > 0
+    mismatch = (v32 != v64).sum() / v64.sum()
+    assert mismatch <= 1e-4, mismatch
+    # registration: the counts are the masks' sums, nothing written past the grid
+    counts = torch.zeros((nrows + 1, ncols), dtype=torch.int32, device=dev)
+    opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=spec.confined, precision=C.FP32, window_kb=window_kb)
+    E.track(site, real, rel, opts, grid, counts=counts[:nrows])
+    c = counts.cpu().numpy()
+    assert not c[nrows].any()
+    assert np.array_equal(c[:nrows], v32.sum(axis=0))
+
+
 def _track(site, real, spec, grid, precision, release=None, head64=False):
     """One oneka_track call: host counts, registered count, and per-trace
     endpoint / naccept / nattempt / status."""
