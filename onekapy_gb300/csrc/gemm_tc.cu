@@ -26,6 +26,14 @@
 //     epilogue of one tile overlaps the MMAs of the next.  Sixteen warps keep
 //     the epilogue's latencies (TMEM loads, the sigmoid, the column-sum
 //     shuffles) hidden.
+// Pairs (CL = 2): when the output has an even number of M tiles, a launch
+// runs clusters of two CTAs on two SMs, which work on the M tiles 2j and
+// 2j + 1 of the same N tile at once.  Each CTA loads its own A slice and one
+// half of the shared B slice; the B half goes to both CTAs' shared memory by
+// TMA multicast, so each SM reads 32 KB from L2 per 64-wide K step instead
+// of 48 KB (the kernel is bound by L2 -> SM bandwidth).  A ring stage is
+// refilled only when both CTAs' MMAs have read it: each MMA issuer's commit
+// arrives on the "empty" barrier of both CTAs.
 // Every mbarrier wait is bounded by the global timer: on a timeout the
 // kernel records an error, waits (bounded) for its own copies and MMAs in
 // flight, frees its tensor memory and returns.
@@ -69,18 +77,22 @@ struct TcArgs {
     int kper;             // K tiles (of TK) per slice
 };
 
-// Work item w of a launch: output tile w % tiles, K slice w / tiles (K tiles
-// [kb, ke)).  The tiles run M fastest, so consecutive items reuse B slices.
+// Work item w of a launch (of a CTA pair when CL = 2): output tile group
+// w % groups, K slice w / groups (K tiles [kb, ke)).  A group is CL tiles
+// along M of one N tile; the CTA of cluster rank `rank` takes the group's
+// tile `rank`.  Groups run M fastest, so consecutive items reuse B slices.
 struct TcItem {
     int m0, n0, kb, ke, slice;
 };
 
-__device__ __forceinline__ TcItem tc_item(const TcArgs& g, int w, int mt, int tiles, int ktiles) {
+template <int CL>
+__device__ __forceinline__ TcItem tc_item(const TcArgs& g, int w, int mt, int groups, int ktiles, int rank) {
     TcItem it;
-    const int t = w % tiles;
-    it.slice = w / tiles;
-    it.m0 = (t % mt) * TM;
-    it.n0 = (t / mt) * TN;
+    const int t = w % groups;
+    const int mg = mt / CL;
+    it.slice = w / groups;
+    it.m0 = ((t % mg) * CL + rank) * TM;
+    it.n0 = (t / mg) * TN;
     it.kb = it.slice * g.kper;
     it.ke = min(ktiles, it.kb + g.kper);
     return it;
@@ -154,6 +166,29 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// The same copy written to shared memory at the same offset in every CTA of
+// the cluster named in `mask`, completing bytes on each one's barrier there.
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
+                                               uint16_t mask) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+        " [%0], [%1, {%2, %3}], [%4], %5;"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask)
+        : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Every thread of every CTA of the cluster.
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor of a K-major tile written by TMA with the
 // 128-byte swizzle: rows of 128 bytes (64 BF16), 8-row swizzle atoms of
 // 1024 bytes (stride-dimension offset), version 1, swizzle mode 2 (128 B).
@@ -182,6 +217,14 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// Arrive on the barrier at this offset in every CTA of `mask` once the MMAs
+// issued so far have completed.
+__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(bar), "h"(mask)
                  : "memory");
 }
 
@@ -216,7 +259,7 @@ __device__ __forceinline__ float warp_colsum16(float (&v)[16], int lane) {
     return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
-template <int EPI>
+template <int EPI, int CL>
 __global__ void __launch_bounds__(THREADS, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs g) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -226,16 +269,20 @@ __global__ void __launch_bounds__(THREADS, 1)
     __shared__ int issued, consumed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN, tiles = mt * nt;
+    const int mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN, groups = (mt / CL) * nt;
     const int ktiles = g.K / TK;
-    const int items = tiles * g.ksplit;
+    const int items = groups * g.ksplit;
+    // this CTA's place: cluster `cid` of `ncl`, rank `rank` in it
+    const int rank = CL > 1 ? (int)cluster_rank() : 0;
+    const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;
+    constexpr uint16_t kPair = (uint16_t)((1u << CL) - 1u);
     unsigned char* base = tc_smem + ((1024u - (smem_addr(tc_smem) & 1023u)) & 1023u);
     const uint32_t sA = smem_addr(base), sB = sA + STAGES * A_BYTES;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(smem_addr(&full[s]), 1);
-            mbar_init(smem_addr(&empty[s]), 1);
+            mbar_init(smem_addr(&empty[s]), CL);       // one commit from each CTA's MMA issuer
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_addr(&acc_full[b]), 1);
@@ -253,6 +300,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    if (CL > 1) cluster_sync();      // the peer's barriers are initialised before any copy reaches them
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
     volatile int* abort_v = &abort_flag;
@@ -261,16 +309,20 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {
             // producer: TMA slices of A and B into the ring, tile after tile
             int it = 0;
-            for (int w = blockIdx.x; w < items && !*abort_v; w += gridDim.x) {
-                const TcItem c = tc_item(g, w, mt, tiles, ktiles);
+            for (int w = cid; w < items && !*abort_v; w += ncl) {
+                const TcItem c = tc_item<CL>(g, w, mt, groups, ktiles, rank);
                 int kt = c.kb;
                 for (; kt < c.ke; ++kt, ++it) {
                     const int s = it % STAGES;
                     if (it >= STAGES && !mbar_wait(smem_addr(&empty[s]), ((it / STAGES) - 1) & 1, abort_v)) break;
                     const uint32_t bar = smem_addr(&full[s]);
-                    mbar_expect_tx(bar, STAGE_BYTES);
+                    mbar_expect_tx(bar, STAGE_BYTES);      // A, and both halves of B when CL = 2
                     tma_load_2d(sA + s * A_BYTES, &tmA, kt * TK, c.m0, bar);
-                    tma_load_2d(sB + s * B_BYTES, &tmB, kt * TK, c.n0, bar);
+                    if (CL > 1)
+                        tma_load_2d_mc(sB + s * B_BYTES + rank * (B_BYTES / CL), &tmB, kt * TK,
+                                       c.n0 + rank * (TN / CL), bar, kPair);
+                    else
+                        tma_load_2d(sB + s * B_BYTES, &tmB, kt * TK, c.n0, bar);
                     issued = it + 1;
                 }
                 if (kt < c.ke) break;
@@ -280,8 +332,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {
             // MMA issuer: tile tl of this CTA accumulates in buffer tl & 1
             int it = 0, tl = 0;
-            for (int w = blockIdx.x; w < items && !*abort_v; w += gridDim.x, ++tl) {
-                const TcItem c = tc_item(g, w, mt, tiles, ktiles);
+            for (int w = cid; w < items && !*abort_v; w += ncl, ++tl) {
+                const TcItem c = tc_item<CL>(g, w, mt, groups, ktiles, rank);
                 const int b = tl & 1, u = tl >> 1;
                 if (tl >= 2 && !mbar_wait(smem_addr(&acc_empty[b]), (u - 1) & 1, abort_v)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -295,7 +347,10 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                     for (int kk = 0; kk < TK / 16; ++kk)   // +32 bytes of K per MMA: +2 in the encoded address
                         mma_bf16(acc, ad + 2 * kk, bd + 2 * kk, (kt > c.kb || kk > 0) ? 1u : 0u);
-                    mma_commit(smem_addr(&empty[s]));
+                    if (CL > 1)
+                        mma_commit_mc(smem_addr(&empty[s]), kPair);   // frees the stage in both CTAs
+                    else
+                        mma_commit(smem_addr(&empty[s]));
                     consumed = it + 1;
                 }
                 if (kt < c.ke) break;
@@ -311,14 +366,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         // 32q .. 32q + 31), columns [cb, cb + 64) of the tile
         const int q = warp & 3, cb = ((warp - 2) >> 2) * 64;
         int tl = 0;
-        for (int w = blockIdx.x; w < items; w += gridDim.x, ++tl) {
+        for (int w = cid; w < items; w += ncl, ++tl) {
             const int b = tl & 1, u = tl >> 1;
             int okw = 0;
             if (lane == 0) okw = mbar_wait(smem_addr(&acc_full[b]), u & 1, abort_v) ? 1 : 0;
             okw = __shfl_sync(0xffffffffu, okw, 0);      // warp-uniform (tcgen05.ld is warp-collective)
             if (!okw) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const TcItem ci = tc_item(g, w, mt, tiles, ktiles);
+            const TcItem ci = tc_item<CL>(g, w, mt, groups, ktiles, rank);
             const int m0 = ci.m0, n0 = ci.n0;
             const float* bias = ci.slice == 0 ? g.bias : nullptr;   // a split product adds the bias once
             const int row = m0 + q * 32 + lane;
@@ -423,6 +478,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    // neither CTA of a pair leaves while the other's copies or commits may
+    // still reach its shared memory
+    if (CL > 1) cluster_sync();
 }
 
 int sm_count() {
@@ -474,13 +532,87 @@ bool gemm_tc_eligible(int a_kmajor, int b_kmajor, int K, int splitk) {
     return a_kmajor && b_kmajor && K % TK == 0 && K > 0 && encode_fn() != nullptr;
 }
 
+namespace {
+
+// Clusters of CL CTAs (each alone on its SM) that can be resident at once for
+// this kernel, cached per kernel; 0 when the query fails.
+template <int EPI, int CL>
+int resident_clusters(cudaStream_t s) {
+    static int n[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 0;
+    if (n[dev] == 0) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = CL;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(CL * sm_count());
+        cfg.blockDim = dim3(THREADS);
+        cfg.dynamicSmemBytes = SMEM_BYTES;
+        cfg.stream = s;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int v = 0;
+        if (cudaOccupancyMaxActiveClusters(&v, gemm_tc_kernel<EPI, CL>, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            v = -1;
+        }
+        n[dev] = v;
+    }
+    return n[dev] > 0 ? n[dev] : 0;
+}
+
+template <int EPI>
+cudaError_t launch_tc(const CUtensorMap& ta, const void* B, int N, int K, int ldb, const TcArgs& g, bool pairs,
+                      cudaStream_t s) {
+    const int mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN;
+    cudaError_t e;
+    if (pairs && mt % 2 == 0) {
+        e = cudaFuncSetAttribute(gemm_tc_kernel<EPI, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        const int clusters = resident_clusters<EPI, 2>(s);
+        if (clusters > 0) {
+            CUtensorMap tb;     // B in half tiles: each CTA of a pair loads one half
+            if (!make_map(&tb, B, N, K, ldb, TN / 2)) return cudaErrorInvalidValue;
+            const int items = (mt / 2) * nt * g.ksplit;
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = 2;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(2 * (items < clusters ? items : clusters));
+            cfg.blockDim = dim3(THREADS);
+            cfg.dynamicSmemBytes = SMEM_BYTES;
+            cfg.stream = s;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            e = cudaLaunchKernelEx(&cfg, gemm_tc_kernel<EPI, 2>, ta, tb, g);
+            return e != cudaSuccess ? e : cudaGetLastError();
+        }
+    }
+    CUtensorMap tb;
+    if (!make_map(&tb, B, N, K, ldb, TN)) return cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(gemm_tc_kernel<EPI, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    const int items = mt * nt * g.ksplit;
+    gemm_tc_kernel<EPI, 1><<<items < sm_count() ? items : sm_count(), THREADS, SMEM_BYTES, s>>>(ta, tb, g);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 // epi: 0 FP32 C, 1 GELU (C = H bf16, Z bf16), 2 sigmoid column sums into
 // sigsum; splitk > 1 (FP32 C only): K is cut into splitk slices whose partial
-// products are added into C, which the caller has zeroed.
+// products are added into C, which the caller has zeroed.  pairs: allow the
+// CTA-pair form (taken when the output has an even number of M tiles).
 cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int epi, const float* bias,
-                           void* Z, float* sigsum, int M, int N, int K, int splitk, cudaStream_t s) {
-    CUtensorMap ta, tb;
-    if (!make_map(&ta, A, M, K, lda, TM) || !make_map(&tb, B, N, K, ldb, TN)) return cudaErrorInvalidValue;
+                           void* Z, float* sigsum, int M, int N, int K, int splitk, int pairs, cudaStream_t s) {
+    CUtensorMap ta;
+    if (!make_map(&ta, A, M, K, lda, TM)) return cudaErrorInvalidValue;
     TcArgs g;
     g.C = C;
     g.Z = (__nv_bfloat16*)Z;
@@ -493,21 +625,11 @@ cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void*
     g.kper = (ktiles + splitk - 1) / splitk;
     g.ksplit = (ktiles + g.kper - 1) / g.kper;        // no empty slice
     if (g.ksplit > 1) epi = kEpiF32Add;
-    const int items = ((N + TN - 1) / TN) * ((M + TM - 1) / TM) * g.ksplit;
-    dim3 grid(items < sm_count() ? items : sm_count());
-#define ONEKA_TC_CASE(E)                                                                                    \
-    {                                                                                                       \
-        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                             SMEM_BYTES);                                                   \
-        if (e != cudaSuccess) return e;                                                                     \
-        gemm_tc_kernel<E><<<grid, THREADS, SMEM_BYTES, s>>>(ta, tb, g);                                     \
-    }
-    if (epi == kEpiF32) ONEKA_TC_CASE(kEpiF32)
-    else if (epi == kEpiF32Add) ONEKA_TC_CASE(kEpiF32Add)
-    else if (epi == kEpiGelu) ONEKA_TC_CASE(kEpiGelu)
-    else ONEKA_TC_CASE(kEpiSigsum)
-#undef ONEKA_TC_CASE
-    return cudaGetLastError();
+    const bool pr = pairs != 0;
+    if (epi == kEpiF32) return launch_tc<kEpiF32>(ta, B, N, K, ldb, g, pr, s);
+    if (epi == kEpiF32Add) return launch_tc<kEpiF32Add>(ta, B, N, K, ldb, g, pr, s);
+    if (epi == kEpiGelu) return launch_tc<kEpiGelu>(ta, B, N, K, ldb, g, pr, s);
+    return launch_tc<kEpiSigsum>(ta, B, N, K, ldb, g, pr, s);
 }
 
 // Read and clear the device error flag of the tensor-core GEMM (synchronizes).

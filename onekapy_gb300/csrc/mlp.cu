@@ -538,12 +538,13 @@ unsigned grid_for(long long n, int per) {
 
 bool gemm_tc_eligible(int a_kmajor, int b_kmajor, int K, int splitk);
 cudaError_t launch_gemm_tc(const void* A, int lda, const void* B, int ldb, void* C, int ldc, int epi, const float* bias,
-                           void* Z, float* sigsum, int M, int N, int K, int splitk, cudaStream_t s);
+                           void* Z, float* sigsum, int M, int N, int K, int splitk, int pairs, cudaStream_t s);
 
 // Which kernel a GEMM runs on: 1 the tcgen05 kernel (gemm_tc.cu), 0 the
 // mma.sync kernel below.  The tcgen05 kernel takes K-major operands with K a
 // multiple of 64, for the FP32 (also split-K), GELU and sigmoid-sum
-// epilogues; bit 0 of `flags` forces the mma.sync kernel.
+// epilogues; bit 0 of `flags` forces the mma.sync kernel, bit 1 keeps the
+// tcgen05 kernel to one CTA per tile (no CTA pairs).
 int gemm_path(int a_kmajor, int b_kmajor, int K, int splitk, int c_f32, int gelu, void* Z, float* sigsum, int flags) {
     if (flags & 1) return 0;
     if (!gemm_tc_eligible(a_kmajor, b_kmajor, K, splitk)) return 0;
@@ -557,7 +558,7 @@ cudaError_t launch_gemm_bf16(const void* A, int lda, int a_kmajor, const void* B
                              int splitk, float* sigsum, int flags, cudaStream_t s) {
     if (gemm_path(a_kmajor, b_kmajor, K, splitk, c_f32, gelu, Z, sigsum, flags))
         return launch_gemm_tc(A, lda, B, ldb, C, ldc, sigsum ? 2 : (gelu ? 1 : 0), bias, Z, sigsum, M, N, K, splitk,
-                              s);
+                              (flags & 2) ? 0 : 1, s);
     GemmArgs g;
     g.A = (const __nv_bfloat16*)A;
     g.B = (const __nv_bfloat16*)B;

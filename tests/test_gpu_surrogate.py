@@ -39,6 +39,55 @@ def test_gemm_layouts_match_fp32(flags, a_kmajor, b_kmajor, M, N, K, splitk):
     assert torch.allclose(Cf, ref, rtol=1e-3, atol=1e-3 * math.sqrt(K)), float((Cf - ref).abs().max())
 
 
+@pytest.mark.parametrize("M,N,K,splitk,epi", [(512, 4096, 512, 1, "f32"), (384, 768, 128, 1, "f32"),
+                                               (512, 1024, 4096, 4, "f32"), (1024, 1536, 512, 1, "gelu"),
+                                               (2048, 4096, 512, 1, "sigsum"), (136, 520, 64, 1, "f32")])
+def test_tcgen05_cta_pairs_match_single_ctas(M, N, K, splitk, epi):
+    """The tcgen05 GEMM in CTA pairs (clusters of two sharing the B slice by
+    TMA multicast; taken when M has an even number of 128-row tiles) against
+    the same kernel one CTA per tile (flags bit 1): the same accumulation,
+    so identical results (split-K adds its slices atomically: within
+    rounding), and both against an FP32 product."""
+    dev = C.device()
+    g = torch.Generator(device="cpu").manual_seed(M + 7 * N + K)
+    A = (torch.randn((M, K), generator=g) / math.sqrt(K)).to(dev).to(torch.bfloat16)
+    W = torch.randn((N, K), generator=g).to(dev).to(torch.bfloat16)
+    b = torch.randn(N, generator=g).to(dev)
+    z = A.float() @ W.float().T + b
+    out = {}
+    for flags in (0, 2):
+        if epi == "f32":
+            Cf = torch.zeros((M, N), dtype=torch.float32, device=dev)
+            SG.gemm(A, True, W, True, Cf, M, N, K, bias=b if splitk == 1 else None, splitk=splitk, flags=flags)
+            out[flags] = (Cf,)
+        elif epi == "gelu":
+            H = torch.empty((M, N), dtype=torch.bfloat16, device=dev)
+            Z = torch.empty_like(H)
+            SG.gemm(A, True, W, True, H, M, N, K, bias=b, gelu=True, Z=Z, flags=flags)
+            out[flags] = (H, Z)
+        else:
+            ss = torch.zeros(N, dtype=torch.float32, device=dev)
+            C.check(C.load().oneka_gemm_bf16_sigmoid_colsum(C.ptr(A), K, C.ptr(W), K, C.ptr(b), C.ptr(ss), M, N, K,
+                                                             flags, C.stream_ptr()))
+            out[flags] = (ss,)
+        torch.cuda.synchronize()
+        assert SG.tc_status() == 0
+    for x, y in zip(out[0], out[2]):
+        if splitk > 1 or epi == "sigsum":     # atomic additions in another order
+            assert torch.allclose(x, y, rtol=1e-5, atol=1e-4), float((x - y).abs().max())
+        else:
+            assert torch.equal(x, y), float((x.float() - y.float()).abs().max())
+    if epi == "f32":
+        ref = z if splitk == 1 else z - b
+        assert torch.allclose(out[0][0], ref, rtol=1e-3, atol=2e-3), float((out[0][0] - ref).abs().max())
+    elif epi == "gelu":
+        assert torch.allclose(out[0][1].float(), z, rtol=2e-2, atol=2e-2)
+        assert torch.allclose(out[0][0].float(), torch.nn.functional.gelu(z), rtol=2e-2, atol=2e-2)
+    else:
+        ref = torch.sigmoid(z).sum(0)
+        assert torch.allclose(out[0][0], ref, rtol=1e-3, atol=1e-2), float((out[0][0] - ref).abs().max())
+
+
 @pytest.mark.parametrize("rows,cols,lds,ldd", [(512, 65536, 65536, 512), (96, 200, 208, 104), (7, 13, 16, 8),
                                                (130, 64, 64, 136)])
 def test_transpose_bf16(rows, cols, lds, ldd):
