@@ -61,7 +61,11 @@ constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int A_BYTES = TM * TK * 2;          // 16 KB
 constexpr int B_BYTES = TN * TK * 2;          // 32 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + alignment slack (1024-byte swizzle atoms)
+// Each epilogue warp's staging area for the FP32 stores: its 32 rows x 16
+// columns, so that a store instruction writes 8 rows x 64 contiguous bytes
+// instead of 32 rows x 16 bytes (whole 32-byte sectors, half the requests).
+constexpr int EPI_STAGE_FLOATS = 32 * 16;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_WARPS * EPI_STAGE_FLOATS * 4 + 1024;   // + alignment slack
 constexpr int TMEM_COLS = 512;       // two 256-column accumulators
 constexpr unsigned long long kWaitNs = 2000000000ull;      // 2 s per wait
 
@@ -175,6 +179,13 @@ __device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* 
         " [%0], [%1, {%2, %3}], [%4], %5;"
         ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask)
         : "memory");
+}
+
+// Bring a tile of the tensor into L2 (no shared memory, no barrier).
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
+    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];"
+                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y)
+                 : "memory");
 }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -311,6 +322,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             int it = 0;
             for (int w = cid; w < items && !*abort_v; w += ncl) {
                 const TcItem c = tc_item<CL>(g, w, mt, groups, ktiles, rank);
+                // The next item's slices into L2 while this one streams: the
+                // CTAs that share a B slice reach it together, and without
+                // this each of its K steps waits for DRAM.
+                if (w + ncl < items) {
+                    const TcItem n = tc_item<CL>(g, w + ncl, mt, groups, ktiles, rank);
+                    for (int k = n.kb; k < n.ke; ++k) {
+                        tma_prefetch_2d(&tmA, k * TK, n.m0);
+                        tma_prefetch_2d(&tmB, k * TK, n.n0 + rank * (TN / CL));
+                    }
+                }
                 int kt = c.kb;
                 for (; kt < c.ke; ++kt, ++it) {
                     const int s = it % STAGES;
@@ -377,21 +398,28 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int m0 = ci.m0, n0 = ci.n0;
             const float* bias = ci.slice == 0 ? g.bias : nullptr;   // a split product adds the bias once
             const int row = m0 + q * 32 + lane;
+            const bool rows_in = m0 + q * 32 + 32 <= g.M;          // the warp's 32 rows all exist
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TN);
 #pragma unroll 1
             for (int c = cb; c < cb + 64; c += 16) {
                 const int nc = n0 + c;
                 if (nc >= g.N) break;                        // uniform across the warp
                 const bool whole = nc + 16 <= g.N;
+                // the bias of these columns is requested before the tensor-memory
+                // load, so the two latencies overlap
+                float4 bq[4];
+                if (bias && whole) {
+                    const float4* bp = reinterpret_cast<const float4*>(bias + nc);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) bq[j] = __ldg(bp + j);
+                }
                 float v[16];
                 tmem_ld16(trow + c, v);
                 if (bias) {
                     if (whole) {
-                        const float4* bp = reinterpret_cast<const float4*>(bias + nc);
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
-                            const float4 bb = __ldg(bp + j);
-                            v[4 * j] += bb.x; v[4 * j + 1] += bb.y; v[4 * j + 2] += bb.z; v[4 * j + 3] += bb.w;
+                            v[4 * j] += bq[j].x; v[4 * j + 1] += bq[j].y; v[4 * j + 2] += bq[j].z; v[4 * j + 3] += bq[j].w;
                         }
                     } else {
 #pragma unroll
@@ -400,12 +428,41 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                 }
                 if (EPI == kEpiSigsum) {
+                    // sigmoid with the hardware exponential and reciprocal (each
+                    // within 2 ulp; a correctly rounded division here cost the
+                    // epilogue most of its issue slots)
+                    if (rows_in) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] = row < g.M ? 1.0f / (1.0f + __expf(-v[j])) : 0.0f;
+                        for (int j = 0; j < 16; ++j) v[j] = __fdividef(1.0f, 1.0f + __expf(-v[j]));
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) v[j] = row < g.M ? __fdividef(1.0f, 1.0f + __expf(-v[j])) : 0.0f;
+                    }
                     const float sum = warp_colsum16(v, lane);
                     const int col = nc + 8 * ((lane >> 4) & 1) + 4 * ((lane >> 3) & 1) + 2 * ((lane >> 2) & 1) +
                                     ((lane >> 1) & 1);
                     if ((lane & 1) == 0 && col < g.N) atomicAdd(g.sigsum + col, sum);
+                } else if ((EPI == kEpiF32 || EPI == kEpiF32Add) && whole && rows_in) {
+                    // row `lane` goes to the staging area (float4 k of row r in
+                    // slot k ^ ((r >> 1) & 3): conflict-free), then lanes 4i..4i+3
+                    // store row 4i + t, 16 columns, for t = 0..3
+                    float4* st = reinterpret_cast<float4*>(base + STAGES * STAGE_BYTES) + (warp - 2) * (EPI_STAGE_FLOATS / 4);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        st[lane * 4 + (k ^ ((lane >> 1) & 3))] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                    __syncwarp();
+                    const int j = lane & 3;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int r = (lane & ~3) + t;
+                        const float4 x = st[r * 4 + (j ^ ((r >> 1) & 3))];
+                        float* Cp = reinterpret_cast<float*>(g.C) + (long long)(m0 + q * 32 + r) * g.ldc + nc + 4 * j;
+                        if (EPI == kEpiF32Add)
+                            atomicAdd(reinterpret_cast<float4*>(Cp), x);
+                        else
+                            *reinterpret_cast<float4*>(Cp) = x;
+                    }
+                    __syncwarp();
                 } else if (row < g.M) {
                     const long long off = (long long)row * g.ldc + nc;
                     if (EPI == kEpiF32Add) {
