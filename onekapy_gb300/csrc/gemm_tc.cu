@@ -181,13 +181,6 @@ __device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* 
         : "memory");
 }
 
-// Bring a tile of the tensor into L2 (no shared memory, no barrier).
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
-    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];"
-                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y)
-                 : "memory");
-}
-
 __device__ __forceinline__ uint32_t cluster_rank() {
     uint32_t r;
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -325,13 +318,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                 // The next item's slices into L2 while this one streams: the
                 // CTAs that share a B slice reach it together, and without
                 // this each of its K steps waits for DRAM.
-                if (w + ncl < items) {
-                    const TcItem n = tc_item<CL>(g, w + ncl, mt, groups, ktiles, rank);
-                    for (int k = n.kb; k < n.ke; ++k) {
-                        tma_prefetch_2d(&tmA, k * TK, n.m0);
-                        tma_prefetch_2d(&tmB, k * TK, n.n0 + rank * (TN / CL));
-                    }
-                }
                 int kt = c.kb;
                 for (; kt < c.ke; ++kt, ++it) {
                     const int s = it % STAGES;
