@@ -368,8 +368,10 @@ ONEKA_API int oneka_count_histogram(const int32_t* counts, int64_t n, int32_t nb
  *
  * K-major A and B with K % 64 == 0 run on the tcgen05 kernel (TMA-staged
  * operands, accumulator in tensor memory; FP32 C, also split-K, or BF16 C
- * with GELU and Z); everything else on an mma.sync kernel.  flags bit 0
- * forces the mma.sync kernel.
+ * with GELU and Z); everything else on an mma.sync kernel.  An output with
+ * an even number of 128-row tiles runs on clusters of two CTAs that share
+ * each B slice by TMA multicast.  flags bit 0 forces the mma.sync kernel;
+ * bit 1 keeps the tcgen05 kernel to one CTA per tile.
  */
 ONEKA_API int oneka_gemm_bf16(const void* A, int32_t lda, int32_t a_kmajor, const void* B, int32_t ldb,
                               int32_t b_kmajor, void* C, int32_t ldc, int32_t c_f32, const float* bias,
