@@ -55,6 +55,103 @@ __global__ void __launch_bounds__(256) register_counts_kernel(uint32_t* __restri
     register_slot(slots + (long long)blockIdx.x * slot_words, mask_words, nrows, ncols, wpr, counts);
 }
 
+// Register nslots slots column by column: the thread of (word w, slot range
+// blockIdx.y) sums bit b of word w over the slots of its range in bit-sliced
+// counters (plane i holds bit i of every one of the 32 column counts; 16
+// planes count to 65,535), clears the words it read, and adds each nonzero
+// column count with one reduction.  A block first lists the slots of its
+// range whose headers (the rows they marked) meet its rows, so untouched
+// rows are neither read nor tested; its threads then load those slots' words
+// eight at a time.  The reductions fall from one per visited node
+// (register_slot) to one per column and slot range.
+constexpr int kColumnsSlotsPerRange = 1024;
+
+__global__ void __launch_bounds__(256) register_columns_kernel(uint32_t* __restrict__ slots, long long slot_words,
+                                                               long long mask_words, int nslots, int nrows,
+                                                               int ncols, int wpr, int32_t* __restrict__ counts) {
+    __shared__ int list[kColumnsSlotsPerRange];
+    __shared__ int nlist;
+    const long long nw = (long long)nrows * wpr;
+    const long long wb = (long long)blockIdx.x * blockDim.x;
+    const long long w = wb + threadIdx.x;
+    const bool valid = w < nw;
+    const int row = valid ? (int)(w / wpr) : 0;
+    const int rfirst = (int)(wb / wpr);
+    const int rlast = (int)((min(nw, wb + blockDim.x) - 1) / wpr);
+    const int r0 = blockIdx.y * kColumnsSlotsPerRange;
+    const int r1 = min(nslots, r0 + kColumnsSlotsPerRange);
+    if (threadIdx.x == 0) nlist = 0;
+    __syncthreads();
+    for (int r = r0 + (int)threadIdx.x; r < r1; r += blockDim.x) {
+        const uint32_t* sl = slots + (long long)r * slot_words;
+        const uint32_t h0 = sl[mask_words], h1 = sl[mask_words + 1];
+        // rows [nrows - h0, h1 - 1] (a zero header: an empty slot)
+        const int rlo = h0 > (uint32_t)nrows ? 0 : nrows - (int)h0;
+        const int rhi = h1 > (uint32_t)nrows ? nrows - 1 : (int)h1 - 1;
+        if (h1 != 0u && rlo <= rlast && rhi >= rfirst) list[atomicAdd(&nlist, 1)] = r;
+    }
+    __syncthreads();
+    const int n = nlist;
+    if (!valid) return;      // no block-wide synchronization below
+    uint32_t plane[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) plane[i] = 0u;
+    uint32_t seen = 0u;
+    for (int m = 0; m < n; m += 8) {
+        uint32_t x[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            x[k] = 0u;
+            if (m + k < n) {
+                const uint32_t* sl = slots + (long long)list[m + k] * slot_words;
+                const uint32_t h0 = sl[mask_words], h1 = sl[mask_words + 1];
+                const int rlo = h0 > (uint32_t)nrows ? 0 : nrows - (int)h0;
+                if (row >= rlo && row < (int)h1) x[k] = 1u;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (x[k]) {
+                uint32_t* p = slots + (long long)list[m + k] * slot_words + w;
+                x[k] = *p;
+                if (x[k]) *p = 0u;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            uint32_t carry = x[k];
+            seen |= carry;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                if (!carry) break;
+                const uint32_t t = plane[i] & carry;
+                plane[i] ^= carry;
+                carry = t;
+            }
+        }
+    }
+    if (!seen) return;
+    const int col0 = (int)(w % wpr) * 32;
+    const int nb = min(32, ncols - col0);      // bits past the last column are never counted
+    int32_t* crow = counts + (long long)row * ncols + col0;
+    for (int b = 0; b < nb; ++b) {
+        if (!((seen >> b) & 1u)) continue;
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) c |= (int)((plane[i] >> b) & 1u) << i;
+        atomicAdd(crow + b, c);
+    }
+}
+
+// Clear the headers of nslots slots (after register_columns_kernel has read them).
+__global__ void clear_headers_kernel(uint32_t* __restrict__ slots, long long slot_words, long long mask_words,
+                                     int nslots) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nslots) return;
+    slots[(long long)r * slot_words + mask_words] = 0u;
+    slots[(long long)r * slot_words + mask_words + 1] = 0u;
+}
+
 // Register every slot of a batched launch: block row -> (job, realization).
 __global__ void __launch_bounds__(256) register_batch_kernel(const __grid_constant__ JobTable T) {
     const int row = blockIdx.x;
@@ -225,6 +322,19 @@ unsigned blocks_for(long long n, int per_block) { return (unsigned)((n + per_blo
 cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid& g, int32_t* counts,
                                    cudaStream_t s) {
     if (nslots <= 0) return cudaSuccess;
+    const long long nw = (long long)g.nrows * words_per_row(g.ncols);
+    const long long wblocks = (nw + 255) / 256;
+    const int ranges = (nslots + kColumnsSlotsPerRange - 1) / kColumnsSlotsPerRange;
+    if (nslots >= 64 && wblocks <= 0x7fffffffLL && ranges <= 65535) {
+        // many slots: column by column (one reduction per column and slot range)
+        register_columns_kernel<<<dim3((unsigned)wblocks, (unsigned)ranges), 256, 0, s>>>(
+            slots, slot_words(g), mask_words(g), nslots, g.nrows, g.ncols, words_per_row(g.ncols), counts);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        clear_headers_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, s>>>(slots, slot_words(g), mask_words(g),
+                                                                             nslots);
+        return cudaGetLastError();
+    }
     register_counts_kernel<<<(unsigned)nslots, 256, 0, s>>>(slots, slot_words(g), mask_words(g), g.nrows,
                                                             g.ncols, words_per_row(g.ncols), counts);
     return cudaGetLastError();

@@ -482,6 +482,7 @@ struct RealConst32 {
     Raster32 g;          // grid constants of the chronicle
     int skip;
     int next;            // next particle of this block's chunk
+    unsigned long long counters[8];   // the block's share of OnekaTrackOut.counters
 };
 
 // float4 slots of a block's well arrays: positions [nw] float4, then
@@ -546,7 +547,8 @@ __device__ __forceinline__ bool feval_c(const RealConst32& rc, const float4* wp,
 // row loop.
 template <int BLOCK>
 __device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Particle32& s, const Cold<BLOCK>& c,
-                                         const Chron& ch, uint32_t* relmask, int pbeg) {
+                                         const Chron& ch, uint32_t* relmask, int pbeg,
+                                         unsigned long long* counters) {
     const long long idx = (long long)r * L.npaths + s.p;
     if (c.i(kRlo) != 0x7fffffff) atomicOr(relmask + ((s.p - pbeg) >> 5), 1u << ((s.p - pbeg) & 31));
     if (L.out.endpoint) {
@@ -564,8 +566,8 @@ __device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Part
     if (L.out.status) L.out.status[idx] = s.status;
     if (L.out.nvertices) L.out.nvertices[idx] = c.i(kNv);
     note_rows(ch.slot, L.mask_words, L.grid.nrows, c.i(kRlo), c.i(kRhi));
-    if (L.out.counters)
-        add_counters((long long*)L.out.counters, s.att, c.i(kAcc), (unsigned)c.i(kNtest), (unsigned)c.i(kNatom),
+    if (L.out.counters)     // into the block's shared counters; flushed once per block
+        add_counters((long long*)counters, s.att, c.i(kAcc), (unsigned)c.i(kNtest), (unsigned)c.i(kNatom),
                      s.status, L.grid, L.xt + (double)c.f(kBx0), L.xt + (double)c.f(kBx1), L.yt + (double)c.f(kBy0),
                      L.yt + (double)c.f(kBy1));
 }
@@ -755,6 +757,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     }
     window_clear(ch);
     for (int i = threadIdx.x; i < (per + 31) / 32; i += BLOCK) relmask[i] = 0u;
+    if (threadIdx.x < 8) rc.counters[threadIdx.x] = 0ull;
     __syncthreads();
     if (rc.skip) {
         if (L.out.status)
@@ -769,7 +772,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     while (s.p < pend && !live) {
         live = start32<MODE, BLOCK>(L, r, rc, wp, wq, s, cold);
         if (!live) {
-            finish32<BLOCK>(L, r, s, cold, ch, relmask, pbeg);
+            finish32<BLOCK>(L, r, s, cold, ch, relmask, pbeg, rc.counters);
             s.p = atomicAdd(&rc.next, 1);
         }
     }
@@ -780,7 +783,7 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
         if (!live) continue;
         live = attempt32<MODE, BLOCK>(L, rc, wp, wq, ch, s, r, cold);
         while (!live && s.p < pend) {
-            finish32<BLOCK>(L, r, s, cold, ch, relmask, pbeg);
+            finish32<BLOCK>(L, r, s, cold, ch, relmask, pbeg, rc.counters);
             s.p = atomicAdd(&rc.next, 1);
             if (s.p < pend) live = start32<MODE, BLOCK>(L, r, rc, wp, wq, s, cold);
         }
@@ -804,6 +807,10 @@ __device__ __forceinline__ void block32(const TrackLaunch& L, int k, int chunk, 
     }
     __syncthreads();
     window_flush(ch);
+    // the block's counters in one atomic each (per-particle global atomics on
+    // eight addresses serialized in L2)
+    if (L.out.counters && threadIdx.x < 8 && rc.counters[threadIdx.x])
+        atomicAdd((unsigned long long*)L.out.counters + threadIdx.x, rc.counters[threadIdx.x]);
 }
 
 template <int MODE, int BLOCK, int MINB>

@@ -15,6 +15,8 @@ Reference map (paths within OnekaPy):
 from __future__ import annotations
 
 import ctypes
+import dataclasses
+import functools
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -83,13 +85,20 @@ class Grid:
         """The grid ProbabilityField(spacing, spacing, xo, yo) grows to when
         expanded to [xo - half_x, xo + half_x] x [yo - half_y, yo + half_y]
         (the repeated += / -= of oneka/probabilityfield.py:229-245, so node
-        coordinates equal the reference's)."""
+        coordinates equal the reference's).  The replay is a host loop of a
+        few thousand steps, so results are cached per argument tuple."""
         half_y = half_x if half_y is None else half_y
-        (xmin, ymin, nrows, ncols, _, _), _ = replay_expand(
-            xo, yo, spacing, spacing,
-            np.array([[xo - half_x + 0.5 * spacing, xo + half_x - 0.5 * spacing,
-                       yo - half_y + 0.5 * spacing, yo + half_y - 0.5 * spacing]]))
-        return Grid(xmin, ymin, float(spacing), float(spacing), nrows, ncols)
+        return dataclasses.replace(_window_grid(float(xo), float(yo), float(spacing), float(half_x),
+                                                float(half_y)))
+
+
+@functools.lru_cache(maxsize=256)
+def _window_grid(xo, yo, spacing, half_x, half_y) -> Grid:
+    (xmin, ymin, nrows, ncols, _, _), _ = replay_expand(
+        xo, yo, spacing, spacing,
+        np.array([[xo - half_x + 0.5 * spacing, xo + half_x - 0.5 * spacing,
+                   yo - half_y + 0.5 * spacing, yo + half_y - 0.5 * spacing]]))
+    return Grid(xmin, ymin, spacing, spacing, nrows, ncols)
 
 
 FRAME_DTYPE = np.dtype([("xmin", "<f8"), ("ymin", "<f8"), ("coff", "<i4"), ("roff", "<i4"),

@@ -52,6 +52,26 @@ def _log_realizations(real: E.Realizations, base: float):
         log.info("    coef rng: (%+.4e, %+.4e, %+.4e, %+.4e, %+.4e, %+.4e)", *c)
 
 
+# Geometry a fresh field reaches when expanded to a fixed window: the
+# expansion replays the reference's repeated += / -= one node at a time (a
+# host loop), so the outcome is kept per (spacing, target, window grid).
+_window_fields: dict = {}
+
+
+def _window_field(spacing, xt, yt, grid: E.Grid) -> ProbabilityField:
+    pfield = ProbabilityField(spacing, spacing, xt, yt)
+    key = (float(spacing), float(xt), float(yt), grid.xmin, grid.ymin, grid.nrows, grid.ncols)
+    geo = _window_fields.get(key)
+    if geo is None:
+        pfield.expand(grid.xmin + 0.5 * spacing, grid.xmin + (grid.ncols - 1.5) * spacing,
+                      grid.ymin + 0.5 * spacing, grid.ymin + (grid.nrows - 1.5) * spacing)
+        _window_fields[key] = (pfield.xmin, pfield.xmax, pfield.ymin, pfield.ymax, pfield.nrows, pfield.ncols)
+    else:
+        pfield.xmin, pfield.xmax, pfield.ymin, pfield.ymax, pfield.nrows, pfield.ncols = geo
+        pfield._alloc()
+    return pfield
+
+
 def _check_status(real: E.Realizations):
     st = real.status.cpu().numpy()
     if np.any(st == C.REAL_RANGE):
@@ -86,13 +106,12 @@ def create_stochastic_capturezone(
     if precision == C.FP32 and nrealizations >= 256:
         opts = E.autotune(site, real, release, opts, E.Grid.window(site.xt, site.yt, spacing,
                                                                    window or 2000.0))
-    pfield = ProbabilityField(spacing, spacing, site.xt, site.yt)
     if window is not None:
         grid = E.Grid.window(site.xt, site.yt, spacing, window)
-        pfield.expand(grid.xmin + 0.5 * spacing, grid.xmin + (grid.ncols - 1.5) * spacing,
-                      grid.ymin + 0.5 * spacing, grid.ymin + (grid.nrows - 1.5) * spacing)
+        pfield = _window_field(spacing, site.xt, site.yt, grid)
         frames = None
     else:
+        pfield = ProbabilityField(spacing, spacing, site.xt, site.yt)
         # pass 1: bounding boxes in the reference's order (realization, then path)
         bbs = []
         for a in range(0, nrealizations, chunk):
