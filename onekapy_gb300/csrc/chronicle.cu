@@ -325,8 +325,11 @@ cudaError_t launch_register_counts(uint32_t* slots, int nslots, const OnekaGrid&
     const long long nw = (long long)g.nrows * words_per_row(g.ncols);
     const long long wblocks = (nw + 255) / 256;
     const int ranges = (nslots + kColumnsSlotsPerRange - 1) / kColumnsSlotsPerRange;
-    if (nslots >= 64 && wblocks <= 0x7fffffffLL && ranges <= 65535) {
-        // many slots: column by column (one reduction per column and slot range)
+    if (nslots >= 4096 && wblocks <= 0x7fffffffLL && ranges <= 65535) {
+        // many slots: column by column (one reduction per column and slot range).
+        // Measured on the 10,000-realization site: 48.5 against 50.3 ms for
+        // track + register at 10,000 slots, equal at 2,048, 0.05-0.2 ms
+        // slower at 200-1,000 slots, where the per-slot pass stays.
         register_columns_kernel<<<dim3((unsigned)wblocks, (unsigned)ranges), 256, 0, s>>>(
             slots, slot_words(g), mask_words(g), nslots, g.nrows, g.ncols, words_per_row(g.ncols), counts);
         cudaError_t e = cudaGetLastError();

@@ -143,6 +143,36 @@ def test_fp32_chronicle_at_the_grid_edges(ncols, window_kb):
     assert np.array_equal(c[:nrows], v32.sum(axis=0))
 
 
+@pytest.mark.parametrize("precision", [C.FP32, C.FP64])
+def test_register_column_pass_equals_mask_sums(precision):
+    """Launches of 4,096 slots or more register column by column (bit-sliced
+    sums over slot ranges); their counts equal the per-realization masks of a
+    mark-only run summed on the host, and the slots are left cleared (a
+    second launch on the same scratch gives the same counts)."""
+    spec = S.config2(nreal=4500, npaths=64)
+    site = _site(spec)
+    real = E.realize(site, spec.nreal, seed=4242)
+    dev = site.device
+    sp = spec.spacing
+    grid = E.Grid(site.xt - 100.2 * sp, site.yt - 99.7 * sp, sp, sp, 201, 201)
+    rel = torch.as_tensor(site.release(spec.npaths), device=dev)
+    opts = E.TrackOptions(duration=spec.duration, tol=spec.tol, maxstep=spec.maxstep, umbra=spec.umbra,
+                          confined=spec.confined, precision=precision)
+    words = grid.slot_bytes() // 4
+    masks = torch.zeros((real.n, words), dtype=torch.int32, device=dev)
+    E.track(site, real, rel, opts, grid, mark_only=masks)
+    m = masks.cpu().numpy().view(np.uint32)[:, :grid.nrows * grid.words_per_row]
+    bits = np.unpackbits(m.view(np.uint8), bitorder="little").reshape(real.n, grid.nrows, -1)[:, :, :grid.ncols]
+    want = bits.sum(axis=0, dtype=np.int64)
+    scratch = torch.zeros(grid.slot_bytes() * real.n, dtype=torch.uint8, device=dev)
+    for _ in range(2):
+        counts = torch.zeros((grid.nrows, grid.ncols), dtype=torch.int32, device=dev)
+        E.track(site, real, rel, opts, grid, counts=counts, scratch=scratch)
+        torch.cuda.synchronize()
+        assert np.array_equal(counts.cpu().numpy(), want)
+    assert not scratch.any().item()
+
+
 def _track(site, real, spec, grid, precision, release=None, head64=False):
     """One oneka_track call: host counts, registered count, and per-trace
     endpoint / naccept / nattempt / status."""
