@@ -509,19 +509,28 @@ struct Particle32 {
     float2 k1;           // f at the current point (first stage, FSAL)
 };
 
-// Shared-memory columns of the per-lane cold state: field f of lane t at
-// cold[f * BLOCK + t] (conflict-free).
-enum ColdField { kNv, kAcc, kRlo, kRhi, kNtest, kNatom, kBx0, kBx1, kBy0, kBy1, kFx0, kFy0, kCoff,
-                 kRoff, kNcols, kNrows, kColdFields };
+// The per-lane cold state in shared memory, four fields to a 16-byte quad:
+// quad q of lane t at cold[(q * BLOCK + t) * 4] (a warp's 16-byte accesses
+// are conflict-free), field f in quad f / 4 at component f % 4.  An accepted
+// step reads the four quads with four 16-byte loads and writes back three.
+enum ColdField { kCoff, kRoff, kNcols, kNrows,      // quad 0: the trace's frame (read only)
+                 kFx0, kFy0, kRlo, kRhi,            // quad 1: frame origin; rows the trace marked
+                 kNtest, kNatom, kAcc, kNv,         // quad 2: counts
+                 kBx0, kBx1, kBy0, kBy1,            // quad 3: bounding box
+                 kColdFields };
+enum ColdQuad { kQFrame, kQWin, kQStat, kQBox };
 
 template <int BLOCK>
 struct Cold {
     uint32_t* base;
     __device__ __forceinline__ int& i(ColdField f) const {
-        return reinterpret_cast<int*>(base)[f * BLOCK + threadIdx.x];
+        return reinterpret_cast<int*>(base)[(((int)f >> 2) * BLOCK + threadIdx.x) * 4 + ((int)f & 3)];
     }
     __device__ __forceinline__ float& f(ColdField fld) const {
-        return reinterpret_cast<float*>(base)[fld * BLOCK + threadIdx.x];
+        return reinterpret_cast<float*>(&i(fld))[0];
+    }
+    __device__ __forceinline__ int4& q(ColdQuad k) const {
+        return reinterpret_cast<int4*>(base)[(int)k * BLOCK + threadIdx.x];
     }
 };
 
@@ -572,15 +581,13 @@ __device__ __forceinline__ void finish32(const TrackLaunch& L, int r, const Part
                      L.yt + (double)c.f(kBy1));
 }
 
-template <int BLOCK>
-__device__ __forceinline__ void push_vertex(const TrackLaunch& L, int r, const Particle32& s, const Cold<BLOCK>& c) {
-    const int nv = c.i(kNv);
+// Write the current point as vertex nv of the trace (when vertices are asked for).
+__device__ __forceinline__ void push_vertex(const TrackLaunch& L, int r, const Particle32& s, int nv) {
     if (L.out.vertices && nv < L.out.max_vertices) {
         double* v = L.out.vertices + ((long long)r * L.npaths + s.p) * 2LL * L.out.max_vertices;
         v[2 * nv] = L.xt + ((double)s.ph.x + (double)s.pl.x);
         v[2 * nv + 1] = L.yt + ((double)s.ph.y + (double)s.pl.y);
     }
-    c.i(kNv) = nv + 1;
 }
 
 // Start particle s.p: release point, frame, first velocity (k1).  Returns
@@ -593,28 +600,19 @@ __device__ __forceinline__ bool start32(const TrackLaunch& L, int r, const RealC
     s.ph = make_float2((float)rx, (float)ry);
     s.pl = make_float2((float)(rx - (double)s.ph.x), (float)(ry - (double)s.ph.y));
     const OnekaFrame f = frame_of(L, r, s.p);
-    c.f(kFx0) = (float)(f.xmin - L.xt);
-    c.f(kFy0) = (float)(f.ymin - L.yt);
-    c.i(kCoff) = f.coff;
-    c.i(kRoff) = f.roff;
-    c.i(kNcols) = f.ncols;
-    c.i(kNrows) = f.nrows;
+    c.q(kQFrame) = make_int4(f.coff, f.roff, f.ncols, f.nrows);
+    c.q(kQWin) = make_int4(__float_as_int((float)(f.xmin - L.xt)), __float_as_int((float)(f.ymin - L.yt)),
+                           0x7fffffff, -1);
     s.status = ONEKA_TRACE_OK;
     s.att = 0;
-    c.i(kAcc) = 0;
-    c.i(kNv) = 0;
-    c.i(kRlo) = 0x7fffffff;
-    c.i(kRhi) = -1;
-    c.i(kNtest) = 0;
-    c.i(kNatom) = 0;
+    c.q(kQStat) = make_int4(0, 0, 0, 1);      // the release point is vertex 0
     const double dur = L.opts.duration;
     s.tau_h = (float)dur;
     s.tau_l = (float)(dur - (double)s.tau_h);
     s.dt = 0.1f * (dur > 0.0 ? 1.0f : (dur < 0.0 ? -1.0f : 0.0f));
     const float2 p0 = add2(s.ph, s.pl);
-    c.f(kBx0) = c.f(kBx1) = p0.x;
-    c.f(kBy0) = c.f(kBy1) = p0.y;
-    push_vertex<BLOCK>(L, r, s, c);
+    c.q(kQBox) = make_int4(__float_as_int(p0.x), __float_as_int(p0.x), __float_as_int(p0.y), __float_as_int(p0.y));
+    push_vertex(L, r, s, 0);
     if (!feval_c<MODE>(rc, wp, wq, L.nwells, s.ph, s.pl, s.k1)) {
         s.status = ONEKA_TRACE_DRY;
         return false;
@@ -683,21 +681,27 @@ __device__ __forceinline__ bool attempt32(const TrackLaunch& L, const RealConst3
         two_sum2(s.ph, S, q, e);
         two_sum2(q, add2(s.pl, e), s.ph, s.pl);
         const float2 b = add2(s.ph, s.pl);
+        int4 stat = c.q(kQStat);                 // ntest, natom, accepted steps, vertices
         if (ch.slot) {
-            unsigned ntest = (unsigned)c.i(kNtest), natom = (unsigned)c.i(kNatom);
-            int rlo = c.i(kRlo), rhi = c.i(kRhi);
-            insert32(ch, L.grid.nrows, L.grid.ncols, c.i(kCoff), c.i(kRoff), c.i(kNcols), c.i(kNrows),
-                     c.f(kFx0), c.f(kFy0), rc.g, a.x, a.y, b.x, b.y, ntest, natom, rlo, rhi);
-            c.i(kNtest) = (int)ntest;
-            c.i(kNatom) = (int)natom;
-            c.i(kRlo) = rlo;
-            c.i(kRhi) = rhi;
+            const int4 fr = c.q(kQFrame);        // coff, roff, ncols, nrows
+            const int4 wn = c.q(kQWin);          // fx0, fy0 (float bits), rlo, rhi
+            unsigned ntest = (unsigned)stat.x, natom = (unsigned)stat.y;
+            int rlo = wn.z, rhi = wn.w;
+            insert32(ch, L.grid.nrows, L.grid.ncols, fr.x, fr.y, fr.z, fr.w, __int_as_float(wn.x),
+                     __int_as_float(wn.y), rc.g, a.x, a.y, b.x, b.y, ntest, natom, rlo, rhi);
+            stat.x = (int)ntest;
+            stat.y = (int)natom;
+            reinterpret_cast<int2*>(&c.q(kQWin))[1] = make_int2(rlo, rhi);
         }
-        c.f(kBx0) = fminf(c.f(kBx0), b.x); c.f(kBx1) = fmaxf(c.f(kBx1), b.x);
-        c.f(kBy0) = fminf(c.f(kBy0), b.y); c.f(kBy1) = fmaxf(c.f(kBy1), b.y);
+        int4& bq = c.q(kQBox);
+        const int4 bx = bq;
+        bq = make_int4(__float_as_int(fminf(__int_as_float(bx.x), b.x)), __float_as_int(fmaxf(__int_as_float(bx.y), b.x)),
+                       __float_as_int(fminf(__int_as_float(bx.z), b.y)), __float_as_int(fmaxf(__int_as_float(bx.w), b.y)));
         s.k1 = k;
-        push_vertex<BLOCK>(L, r, s, c);
-        c.i(kAcc) += 1;
+        push_vertex(L, r, s, stat.w);
+        stat.z += 1;
+        stat.w += 1;
+        c.q(kQStat) = stat;
     }
     float fac = __powf(tol / (est + eps), 0.2f);
     const float fstep = maxstep / (ds + eps);
