@@ -315,9 +315,6 @@ __global__ void __launch_bounds__(THREADS, 1)
             int it = 0;
             for (int w = cid; w < items && !*abort_v; w += ncl) {
                 const TcItem c = tc_item<CL>(g, w, mt, groups, ktiles, rank);
-                // The next item's slices into L2 while this one streams: the
-                // CTAs that share a B slice reach it together, and without
-                // this each of its K steps waits for DRAM.
                 int kt = c.kb;
                 for (; kt < c.ke; ++kt, ++it) {
                     const int s = it % STAGES;

@@ -14,8 +14,9 @@
 //     float (the recentred r^2);
 //   * x and y travel together as packed FP32 pairs (Blackwell's FADD2 /
 //     FMUL2 / FFMA2), one instruction for both coordinates;
-//   * the discharge's well terms are summed with Kahan compensation (the
-//     potential's too in the FP64 head-inversion mode);
+//   * the discharge's well terms are summed with Kahan compensation, one
+//     compensated addition per group of four wells (the potential's per
+//     well in the FP64 head-inversion mode);
 //   * the head is inverted from the compensated potential in FP32 (the
 //     inversion is well conditioned; see feval32);
 //   * the time left is a float pair counting down to zero, so no FP64
