@@ -57,9 +57,9 @@ E2E_CALLS = 3           # timed public-API calls averaged into e2e
 TUNE_SAMPLE = 2048      # realizations the autotuner times each launch shape on (several waves)
 SURROGATE_TOLERANCE = 0.01   # judge L-inf bar of the screened field: the tracker's own accuracy bar
 # DRAM bytes per realization of the tracking launch on this site, from one ncu
-# capture of a 1,000-realization launch (dram__bytes_read.sum 15.57 MB +
+# capture of a 1,000-realization launch (dram__bytes_read.sum 15.56 MB +
 # dram__bytes_write.sum 0.07 MB).
-TRACK32_DRAM_BYTES_PER_REALIZATION = (15.566336e6 + 0.068352e6) / 1000
+TRACK32_DRAM_BYTES_PER_REALIZATION = (15.555072e6 + 0.069888e6) / 1000
 
 
 def args_():
