@@ -108,6 +108,21 @@ def test_window_and_release_match_reference(case):
     assert np.array_equal(E.release_ring(xt, yt, rt, int(d["npaths"])), d["release"])
 
 
+def test_window_grid_cache_returns_independent_equal_grids():
+    """Grid.window caches its replay of the reference's expansion; every call
+    returns its own Grid (a caller changing one does not change the next)
+    equal to a fresh replay."""
+    from onekapy_gb300 import engine as E
+    g1 = E.Grid.window(1234.5, -678.25, 5.0, 4000.0)
+    g1.nrows = -1
+    g2 = E.Grid.window(1234.5, -678.25, 5.0, 4000.0)
+    assert g2.nrows == 1601 and g2 is not g1
+    (xmin, ymin, nrows, ncols, _, _), _ = E.replay_expand(
+        1234.5, -678.25, 5.0, 5.0, np.array([[1234.5 - 4000.0 + 2.5, 1234.5 + 4000.0 - 2.5,
+                                              -678.25 - 4000.0 + 2.5, -678.25 + 4000.0 - 2.5]]))
+    assert (g2.xmin, g2.ymin, g2.nrows, g2.ncols) == (xmin, ymin, nrows, ncols)
+
+
 def test_distribution_helpers():
     from onekapy_gb300 import engine as E
     from onekapy_gb300 import stochastic as St
