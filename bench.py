@@ -379,7 +379,10 @@ def run_ours(a):
                         "d2h_bytes_per_step": d2h},
                 "tracker_launch": {"block": o32.block, "occupancy": o32.occupancy,
                                    "window_kb": o32.window_kb, "chosen_by": f"autotune on {min(R, TUNE_SAMPLE)} realizations"},
-                "gpu_launches": 3 * a.steps,
+                # per step: realize, track, and the register pass (column by
+                # column from 4,096 slots: two kernels, the second clearing
+                # the slot headers)
+                "gpu_launches": (2 + (2 if R >= E.REGISTER_COLUMNS_MIN_SLOTS else 1)) * a.steps,
                 "clocks": clocks,
                 "cpu_baseline": cpu}
     if world > 1:

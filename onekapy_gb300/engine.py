@@ -314,6 +314,11 @@ class TrackOptions:
                                 int(self.occupancy), int(bool(self.head64)))
 
 
+# A launch of this many realization slots or more registers its counts column
+# by column (two kernels: the sums, then the slot headers cleared); fewer, one
+# block per slot (csrc/chronicle.cu, kColumnsMinSlots).
+REGISTER_COLUMNS_MIN_SLOTS = 4096
+
 # OnekaTrackOut.counters: attempts, accepted steps, node tests, word ORs, DRY
 # traces, STEP_LIMIT traces, traces that left the grid, (reserved)
 COUNTERS = 8
