@@ -372,8 +372,8 @@ def run_ours(a):
                              "traffic": TRACK32_DRAM_BYTES_PER_REALIZATION * R,
                              "traffic_source": "ncu dram__bytes_read+write of a 1000-realization launch, "
                                                "scaled by realizations",
-                             "kernel": "track32_kernel; time includes the register pass "
-                                       "(register_columns_kernel, 1.5 % of the step), traffic is the tracker's",
+                             "kernel": "track32_kernel; time includes the register pass (1.5 % of "
+                                       "the 10,000-realization step), traffic is the tracker's",
                              "peak_source": "measured FP32 FMA loop on this GPU (oneka_fma_peak)"},
                 "roofline_hbm": _hbm_roofline(TRACK32_DRAM_BYTES_PER_REALIZATION * R, t_track),
                 "e2e": {"value": e2e_n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
